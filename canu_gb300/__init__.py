@@ -1,0 +1,248 @@
+"""GB300 overlapInCore engine -- Python binding of liboic_gpu.so (include/oic_gpu.h).
+
+The compute path is the CUDA library; this module only marshals host buffers through
+ctypes.  There is no CPU fallback: if the library or a CUDA device is missing, every
+call raises OicError.
+
+    from canu_gb300 import Overlapper, default_params
+    p = default_params(kmerLen=22, maxErate=0.06, minOlapLen=500, hashBits=23)
+    with Overlapper(p) as ov:
+        ov.set_reads_seqdb("reads.seqdb")
+        ov.run()
+        recs = ov.overlaps()          # (n, 6) uint32, the ovFile record words
+"""
+import ctypes
+import os
+import struct
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD, "liboic_gpu.so")
+
+OIC_OK, OIC_ERR_ARG, OIC_ERR_INPUT, OIC_ERR_CUDA, OIC_ERR_NOMEM, OIC_ERR_OVERFLOW, OIC_ERR_STATE, OIC_ERR_DEVICE = range(8)
+
+# Exported entry points of include/oic_gpu.h.
+EXPORTS = (
+    "oic_default_params", "oic_create", "oic_destroy", "oic_set_reads", "oic_set_skip_kmers",
+    "oic_load_hash_block", "oic_run_refs", "oic_run", "oic_num_overlaps", "oic_fetch_overlaps",
+    "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
+)
+
+
+class OicError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"oic error {code}: {msg}")
+        self.code = code
+
+
+class OicParams(ctypes.Structure):
+    """oic_params (overlapInCore.H:367-473)."""
+    _fields_ = [
+        ("maxErate", ctypes.c_double), ("alignNoise", ctypes.c_double),
+        ("partial", ctypes.c_int32), ("uniqueOlapPerPair", ctypes.c_int32),
+        ("useHopelessCheck", ctypes.c_int32), ("minKmers", ctypes.c_int32),
+        ("kmerLen", ctypes.c_uint32), ("hashBits", ctypes.c_uint32),
+        ("maxHashLoad", ctypes.c_double), ("maxHashDataLen", ctypes.c_uint64),
+        ("minOlapLen", ctypes.c_int32), ("numThreads", ctypes.c_uint32),
+        ("bgnHashID", ctypes.c_uint32), ("endHashID", ctypes.c_uint32),
+        ("minLibToHash", ctypes.c_uint32), ("maxLibToHash", ctypes.c_uint32),
+        ("bgnRefID", ctypes.c_uint32), ("endRefID", ctypes.c_uint32),
+        ("minLibToRef", ctypes.c_uint32), ("maxLibToRef", ctypes.c_uint32),
+    ]
+
+
+class OicStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "kmerHitsWithoutOlap", "kmerHitsWithOlap", "kmerHitsSkipped", "multiOverlap",
+        "totalOverlaps", "containedOverlaps", "dovetailOverlaps", "badShortWindow", "badLongWindow",
+        "dpCells", "slideBases", "extensions", "seeds", "candidatePairs", "nodes")] + [
+        ("nHashBlocks", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+        ("msHash", ctypes.c_double), ("msSeed", ctypes.c_double),
+        ("msAlign", ctypes.c_double), ("msTotal", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def library():
+    """Load liboic_gpu.so (built in-tree by canu_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OicError(OIC_ERR_CUDA, f"{LIB_PATH} is not built; run python -m canu_gb300.build")
+        lib = ctypes.CDLL(LIB_PATH)
+        P, U32, U64, I32 = ctypes.POINTER, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
+        vp = ctypes.c_void_p
+        lib.oic_default_params.argtypes = [P(OicParams)]
+        lib.oic_create.argtypes = [P(OicParams), ctypes.c_int, P(vp)]
+        lib.oic_destroy.argtypes = [vp]
+        lib.oic_set_reads.argtypes = [vp, U32, vp, vp, vp, vp, U64]
+        lib.oic_set_skip_kmers.argtypes = [vp, ctypes.c_char_p, U64]
+        lib.oic_load_hash_block.argtypes = [vp, U32, U32, P(U32)]
+        lib.oic_run_refs.argtypes = [vp, U32, U32]
+        lib.oic_run.argtypes = [vp]
+        lib.oic_num_overlaps.argtypes = [vp, P(U64)]
+        lib.oic_fetch_overlaps.argtypes = [vp, vp, U64, P(U64)]
+        lib.oic_clear_overlaps.argtypes = [vp]
+        lib.oic_get_stats.argtypes = [vp, P(OicStats)]
+        lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
+        lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
+        lib.oic_last_error.argtypes = [vp]
+        lib.oic_last_error.restype = ctypes.c_char_p
+        _lib = lib
+    return _lib
+
+
+def default_params(**kw):
+    """The reference defaults (oicParameters::initialize) with overrides by field name.
+    Float flags are rounded through float32 as overlapInCore's strtof does."""
+    p = OicParams()
+    library().oic_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        if k in ("maxErate", "alignNoise"):
+            v = float(np.float32(v))
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def read_seqdb(path):
+    """Load an oic_seqdb container: (libID, length, offset, bases) as numpy arrays."""
+    with open(path, "rb") as f:
+        head = f.read(24)
+        if head[:8] != b"OICSEQ01":
+            raise ValueError(f"{path}: not an oic_seqdb container")
+        n, _, nb = struct.unpack("<IIQ", head[8:24])
+        idx = np.frombuffer(f.read(16 * n), dtype=np.dtype([("lib", "<u4"), ("len", "<u4"), ("off", "<u8")]))
+        bases = np.frombuffer(f.read(nb), dtype=np.uint8)
+    return (np.ascontiguousarray(idx["lib"]), np.ascontiguousarray(idx["len"]),
+            np.ascontiguousarray(idx["off"]), bases)
+
+
+def write_seqdb(path, seqs, libs=None):
+    """Write reads (list of str/bytes) as an oic_seqdb container."""
+    seqs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    lens = [len(s) for s in seqs]
+    libs = libs if libs is not None else [1] * len(seqs)
+    with open(path, "wb") as f:
+        f.write(b"OICSEQ01" + struct.pack("<IIQ", len(seqs), 0, sum(lens)))
+        off = 0
+        for lb, ln in zip(libs, lens):
+            f.write(struct.pack("<IIQ", lb, ln, off))
+            off += ln
+        for s in seqs:
+            f.write(s)
+
+
+class Overlapper:
+    """One engine context (one CUDA stream) -- the GPU overlapInCore."""
+
+    def __init__(self, params, device=0):
+        self._lib = library()
+        self._ctx = ctypes.c_void_p()
+        self.params = params
+        rc = self._lib.oic_create(ctypes.byref(params), int(device), ctypes.byref(self._ctx))
+        if rc != OIC_OK:
+            raise OicError(rc, "oic_create failed (invalid parameters or no usable CUDA device)")
+
+    def close(self):
+        if self._ctx:
+            self._lib.oic_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != OIC_OK:
+            raise OicError(rc, self._lib.oic_last_error(self._ctx).decode())
+
+    def set_reads(self, lib, length, offset, bases):
+        lib = np.ascontiguousarray(lib, dtype=np.uint32)
+        length = np.ascontiguousarray(length, dtype=np.uint32)
+        offset = np.ascontiguousarray(offset, dtype=np.uint64)
+        bases = np.ascontiguousarray(bases, dtype=np.uint8)
+        self._keep = (lib, length, offset, bases)
+        self._check(self._lib.oic_set_reads(self._ctx, len(length), _ptr(lib), _ptr(length), _ptr(offset),
+                                            _ptr(bases), bases.size))
+
+    def set_reads_seqdb(self, path):
+        self.set_reads(*read_seqdb(path))
+
+    def set_skip_kmers(self, kmers):
+        k = self.params.kmerLen
+        blob = "".join(kmers).encode() if not isinstance(kmers, (bytes, bytearray)) else bytes(kmers)
+        self._check(self._lib.oic_set_skip_kmers(self._ctx, blob, len(blob) // k))
+
+    def load_hash_block(self, bgn, end):
+        last = ctypes.c_uint32()
+        self._check(self._lib.oic_load_hash_block(self._ctx, bgn, end, ctypes.byref(last)))
+        return last.value
+
+    def run_refs(self, bgn, end):
+        self._check(self._lib.oic_run_refs(self._ctx, bgn, end))
+
+    def run(self):
+        self._check(self._lib.oic_run(self._ctx))
+
+    def overlaps(self):
+        n = ctypes.c_uint64()
+        self._check(self._lib.oic_num_overlaps(self._ctx, ctypes.byref(n)))
+        out = np.zeros((n.value, 6), dtype=np.uint32)
+        got = ctypes.c_uint64()
+        self._check(self._lib.oic_fetch_overlaps(self._ctx, _ptr(out), n.value, ctypes.byref(got)))
+        return out[: got.value]
+
+    def clear(self):
+        self._check(self._lib.oic_clear_overlaps(self._ctx))
+
+    def stats(self):
+        s = OicStats()
+        self._check(self._lib.oic_get_stats(self._ctx, ctypes.byref(s)))
+        return s.as_dict()
+
+    def match_limit(self):
+        n = ctypes.c_uint32()
+        self._check(self._lib.oic_get_match_limit(self._ctx, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        self._check(self._lib.oic_get_match_limit(self._ctx, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def extend_batch(self, sRead, sRev, tRead, mStart, mOffset, mLen):
+        """Batched Extend_Alignment; returns (out[n,5], kind[n], deltaLen[n])."""
+        a = [np.ascontiguousarray(x, dtype=t) for x, t in zip(
+            (sRead, sRev, tRead, mStart, mOffset, mLen),
+            (np.uint32, np.uint32, np.uint32, np.int32, np.int32, np.int32))]
+        n = len(a[0])
+        out = np.zeros((n, 5), dtype=np.int32)
+        kind = np.zeros(n, dtype=np.int32)
+        dl = np.zeros(n, dtype=np.int32)
+        self._check(self._lib.oic_extend_batch(self._ctx, n, *[_ptr(x) for x in a], _ptr(out), _ptr(kind), _ptr(dl)))
+        return out, kind, dl
+
+
+def sort_records(rec):
+    """Records in ovOverlap::operator< order (ovOverlap.H:264-277): a_iid, b_iid, then
+    the data words as two 64-bit values -- the same as lexicographic on the six words."""
+    rec = np.asarray(rec, dtype=np.uint32).reshape(-1, 6)
+    if len(rec) == 0:
+        return rec
+    order = np.lexsort(tuple(rec[:, k] for k in range(5, -1, -1)))
+    return rec[order]

@@ -1,0 +1,109 @@
+"""Build recipe for the GB300 overlap engine and its command-line front end.
+
+    python -m canu_gb300.build          # everything
+    python -m canu_gb300.build --lib    # only liboic_gpu.so
+
+Outputs (git-ignored) go to canu_gb300/_build/:
+    liboic_gpu.so      the C-ABI library (include/oic_gpu.h), sm_103a kernels
+    overlapInCore      the drop-in command line, linked against the library
+    oic_synth          the synthetic read generator
+
+Each translation unit is compiled in parallel; nvcc targets exactly sm_103a.
+"""
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_build")
+CSRC = os.path.join(HERE, "csrc")
+INC = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
+           "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
+CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+    return r.stdout
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hs += [os.path.join(INC, f) for f in os.listdir(INC) if f.endswith(".h")]
+    return hs
+
+
+def build_lib(verbose=False, extra=()):
+    os.makedirs(OUT, exist_ok=True)
+    nv = nvcc()
+    hdrs = _headers()
+    objs = []
+    jobs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(OUT, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + hdrs):
+            jobs.append([nv] + ARCH + NVFLAGS + list(extra) + ["-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=len(CU_SOURCES)) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out.strip():
+                print(out)
+    lib = os.path.join(OUT, "liboic_gpu.so")
+    if _stale(lib, objs):
+        _run([nv] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+    return lib
+
+
+def build_tools():
+    os.makedirs(OUT, exist_ok=True)
+    nv = nvcc()
+    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
+    lib = os.path.join(OUT, "liboic_gpu.so")
+    cli_src = os.path.join(HERE, "host", "overlapInCore.cpp")
+    cli = os.path.join(OUT, "overlapInCore")
+    if _stale(cli, [cli_src, lib] + _headers()):
+        _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", cli, cli_src, "-L" + OUT, "-loic_gpu",
+              "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
+    syn_src = os.path.join(HERE, "synth", "oic_synth.cpp")
+    syn = os.path.join(OUT, "oic_synth")
+    if _stale(syn, [syn_src, os.path.join(INC, "oic_seqdb.h")]):
+        _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", syn, syn_src])
+    return cli, syn
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--lib", action="store_true")
+    ap.add_argument("-v", action="store_true")
+    a = ap.parse_args(argv)
+    print(build_lib(verbose=a.v))
+    if not a.lib:
+        print(*build_tools())
+
+
+if __name__ == "__main__":
+    sys.exit(main())

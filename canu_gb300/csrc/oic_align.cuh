@@ -1,0 +1,385 @@
+// oic_align.cuh -- warp-cooperative banded prefix edit distance (furthest-reaching
+// diagonals) and the per-read-pair driver around it.
+//
+// One warp owns one read pair.  Lanes own diagonals of the current error row (lane l
+// takes d = Lc + l, Lc + l + 32, ...); the previous row lives in a shared-memory
+// buffer, every kept row is appended to the warp's traceback arena in HBM, and the
+// slides compare 32 bases per step on the 2-bit packed reads.  The arithmetic is the
+// reference's exactly -- integer rows, the same band pruning against Edit_Match_Limit,
+// the same first-index tie breaks, and the branch-point test in IEEE double with
+// explicitly rounded multiply / subtract / divide (no FMA contraction), as an x86-64
+// build of canu computes it.
+#pragma once
+
+#include "oic_common.cuh"
+
+namespace oic {
+
+// Per-warp global scratch.
+struct WarpScratch {
+  int  *arena;       // kept DP rows, band-compacted
+  int  *rowOff;      // per error row: arena offset
+  int  *rowL;        // per error row: kept band [rowL, rowR]
+  int  *rowR;
+  int  *deltaL;      // Left_Delta (merged delta of the last extension)
+  int  *deltaR;      // Right_Delta
+  int  *stack;       // Delta_Stack
+  unsigned char *alive;   // match-node alive flags of the current pair
+};
+
+struct AlignCaps {
+  int arenaCap;   // ints per warp
+  int rowCap;     // error rows per warp (also bounds the delta arrays)
+  int nodeCap;    // match nodes per pair
+  int bandW;      // ints per shared-memory row buffer
+};
+
+struct WarpDP {
+  WarpScratch        sc;
+  AlignCaps          cap;
+  int               *smA, *smB;     // shared-memory row buffers (bandW ints each)
+  const int         *eml;           // Edit_Match_Limit
+  DevParams          P;
+  unsigned long long cells, slides;
+  u32                err;           // capacity error of the current pair (0 = ok)
+  int                leftLen, rightLen;
+};
+
+// Row-0 exact slide shared by the warp: each lane tests one 32-base window per step.
+template <int STEP>
+__device__ __forceinline__ int warp_slide0(const SeqView &A, i64 a0, const SeqView &T, i64 t0, int m,
+                                           unsigned long long &slides) {
+  const int lane = threadIdx.x & 31;
+  int       base = 0;
+  while (base < m) {
+    int off = base + lane * 32;
+    int r   = 32;
+    if (off < m) r = match_run32<STEP>(A, a0 + STEP * (i64)off, T, t0 + STEP * (i64)off);
+    unsigned short_ = __ballot_sync(0xffffffffu, off < m && r < 32);
+    if (short_) {
+      int first = __ffs(short_) - 1;
+      int rr    = __shfl_sync(0xffffffffu, r, first);
+      int run   = base + first * 32 + rr;
+      run       = min(run, m);
+      if (lane == 0) slides += (unsigned long long)run;
+      return run;
+    }
+    base += 32 * 32;
+  }
+  if (lane == 0) slides += (unsigned long long)m;
+  return m;
+}
+
+// Traceback of Set_Right_Delta / Set_Left_Delta (prefixEditDistance-forward.C:32-71,
+// -reverse.C:36-93) from row e, diagonal d whose value is `last`.  Lane 0 only.
+// Pushes one entry per indel into out[]; returns the value reached on row 0.
+__device__ __forceinline__ int trace_rows(const WarpDP &w, int e, int d, int last, int *out, int &n) {
+  n = 0;
+  for (int k = e; k > 0; k--) {
+    const int off = w.sc.rowOff[k - 1], L = w.sc.rowL[k - 1], R = w.sc.rowR[k - 1];
+    const int g0 = (d >= L && d <= R) ? w.sc.arena[off + d - L] : -2;
+    const int gm = (d - 1 >= L && d - 1 <= R) ? w.sc.arena[off + d - 1 - L] : -2;
+    const int gp = (d + 1 >= L && d + 1 <= R) ? w.sc.arena[off + d + 1 - L] : -2;
+    int from = d, mx = 1 + g0;
+    if (gm > mx) { from = d - 1; mx = gm; }
+    if (1 + gp > mx) { from = d + 1; mx = 1 + gp; }
+    if (from == d - 1) {
+      out[n++] = mx - last - 1;
+      last     = gm;
+      d--;
+    } else if (from == d + 1) {
+      out[n++] = last - (mx - 1);
+      last     = gp;
+      d++;
+    }
+  }
+  return last;
+}
+
+__device__ __forceinline__ int arena_get(const WarpDP &w, int e, int d) {
+  const int L = w.sc.rowL[e], R = w.sc.rowR[e];
+  return (d >= L && d <= R) ? w.sc.arena[w.sc.rowOff[e] + d - L] : -2;
+}
+
+// Set_Right_Delta (forward.C:32-71) into sc.deltaR; lane 0.
+__device__ __forceinline__ void set_right_delta(WarpDP &w, int e, int d, int last) {
+  int n;
+  int l = trace_rows(w, e, d, last, w.sc.stack, n);
+  w.sc.stack[n++] = l + 1;
+  int k           = 0;
+  for (int i = n - 1; i > 0; i--) {
+    int s = w.sc.stack[i - 1];
+    w.sc.deltaR[k++] = abs(w.sc.stack[i]) * ((s > 0) - (s < 0));
+  }
+  w.rightLen = n - 1;
+}
+
+// Set_Left_Delta (reverse.C:36-93) into sc.deltaL; lane 0.
+__device__ __forceinline__ void set_left_delta(WarpDP &w, int e, int d, int last, int &leftover, int &tEnd, int tLen) {
+  int n;
+  leftover  = trace_rows(w, e, d, last, w.sc.deltaL, n);
+  int *ld   = w.sc.deltaL;
+  if (n > 1 && ld[0] == 1 && tEnd + tLen > 0) {
+    ld[0] = (ld[1] > 0) ? ld[1] + 1 : ld[1] - 1;
+    for (int i = 2; i < n; i++) ld[i - 1] = ld[i];
+    n--;
+    tEnd--;
+    if (n == 0) leftover++;
+  }
+  w.leftLen = n;
+}
+
+// forward() (prefixEditDistance-forward.C:94-314) for STEP = +1 and reverse()
+// (prefixEditDistance-reverse.C:114-330) for STEP = -1, cooperatively by one warp.
+// A[STEP*i] is base a0+STEP*i of view A, T likewise.  Returns the error count; the
+// outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
+template <int STEP>
+__device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
+                              int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
+  const int lane = threadIdx.x & 31;
+  const double BMV = w.P.branchMatchValue;
+
+  if (STEP > 0) w.rightLen = 0;
+  else w.leftLen = 0;
+
+  const int r0 = warp_slide0<STEP>(A, a0, T, t0, m, w.slides);
+  if (r0 == m) {
+    aEnd = tEnd = STEP * m;
+    if (STEP < 0) leftover = m;
+    toEnd = true;
+    return 0;
+  }
+
+  if (lane == 0) {
+    w.sc.arena[0]  = r0;
+    w.sc.rowOff[0] = 0;
+    w.sc.rowL[0]   = 0;
+    w.sc.rowR[0]   = 0;
+  }
+  int *prev = w.smA, *cur = w.smB;
+  if (lane == 0) prev[0] = r0;
+  __syncwarp();
+
+  int    used = 1, prevBase = 0, L = 0, R = 0;
+  int    longest = 0, bestD = 0, bestE = 0, msLen = 0, msD = 0, msE = 0;
+  double maxScore = 0.0;
+  int    e;
+
+  for (e = 1; e <= errorLimit; e++) {
+    if (e >= w.cap.rowCap) { w.err |= kErrRowsFull; return 0; }
+    const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
+    const int width = Rc - Lc + 1;
+    if (width > w.cap.bandW) { w.err |= kErrBandWide; return 0; }
+
+    int myEnd = INT_MAX;
+    for (int d = Lc + lane; d <= Rc; d += 32) {
+      const int p0 = (d >= L && d <= R) ? prev[d - prevBase] : -2;
+      const int pm = (d - 1 >= L && d - 1 <= R) ? prev[d - 1 - prevBase] : -2;
+      const int pp = (d + 1 >= L && d + 1 <= R) ? prev[d + 1 - prevBase] : -2;
+      int row = 1 + p0;
+      if (pm > row) row = pm;
+      if (1 + pp > row) row = 1 + pp;
+      const int lim = min(m - row, n - row - d);
+      if (lim > 0) row += slide<STEP>(A, a0, T, t0, row, d, lim, w.slides);
+      cur[d - Lc] = row;
+      if ((row == m || row + d == n) && d < myEnd) myEnd = d;
+    }
+    __syncwarp();
+    const int dEnd = warp_min(myEnd);
+
+    if (dEnd != INT_MAX) {
+      w.cells += (unsigned long long)(dEnd - Lc + 1);
+      const int    row     = cur[dEnd - Lc];
+      const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
+      const int    tailLen = row - msLen;
+      const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
+      bool abort_ = (w.P.partial && score < maxScore);
+      if (e > 20 / 2 && tailLen >= 20 && slope >= w.P.minBranchTailSlope) abort_ = true;
+      if (abort_) {
+        aEnd = STEP * msLen;
+        tEnd = STEP * (msLen + msD);
+        if (lane == 0) {
+          const int last = arena_get(w, msE, msD);
+          if (STEP > 0) set_right_delta(w, msE, msD, last);
+          else set_left_delta(w, msE, msD, last, leftover, tEnd, n);
+        }
+        if (STEP > 0) w.rightLen = __shfl_sync(0xffffffffu, w.rightLen, 0);
+        else {
+          w.leftLen = __shfl_sync(0xffffffffu, w.leftLen, 0);
+          leftover  = __shfl_sync(0xffffffffu, leftover, 0);
+          tEnd      = __shfl_sync(0xffffffffu, tEnd, 0);
+        }
+        toEnd = false;
+        __syncwarp();
+        return msE;
+      }
+      int d = dEnd;
+      if (STEP > 0) {
+        // Force the last error to be a mismatch (forward.C:215-221).
+        const int pp = (d + 1 >= L && d + 1 <= R) ? prev[d + 1 - prevBase] : -2;
+        if (row == m && 1 + pp == row && d < Rc) d++;
+        aEnd = row;
+        tEnd = row + d;
+        if (lane == 0) set_right_delta(w, e, d, row);
+        w.rightLen = __shfl_sync(0xffffffffu, w.rightLen, 0);
+      } else {
+        aEnd = -row;
+        tEnd = -row - d;
+        if (lane == 0) set_left_delta(w, e, d, row, leftover, tEnd, n);
+        w.leftLen = __shfl_sync(0xffffffffu, w.leftLen, 0);
+        leftover  = __shfl_sync(0xffffffffu, leftover, 0);
+        tEnd      = __shfl_sync(0xffffffffu, tEnd, 0);
+      }
+      toEnd = true;
+      __syncwarp();
+      return e;
+    }
+    w.cells += (unsigned long long)width;
+
+    // Band pruning (forward.C:245-280): the kept band is [first, last] unpruned diagonal.
+    const int lim = w.eml[e];
+    int myL = INT_MAX, myR = INT_MIN;
+    for (int d = Lc + lane; d <= Rc; d += 32) {
+      const int v = cur[d - Lc];
+      if (!(v + max(d, 0) < lim)) {
+        myL = min(myL, d);
+        myR = max(myR, d);
+      }
+    }
+    const int L2 = warp_min(myL);
+    if (L2 == INT_MAX) break;
+    const int R2 = warp_max(myR);
+
+    // Longest row on the kept band, first diagonal on ties (forward.C:284-289).
+    int myV = -1, myD = INT_MAX;
+    for (int d = L2 + lane; d <= R2; d += 32) {
+      const int v = cur[d - Lc];
+      if (v > myV) { myV = v; myD = d; }
+    }
+    const int rowMax = warp_max(myV);
+    const int dMax   = warp_min(myV == rowMax ? myD : INT_MAX);
+    if (rowMax > longest) {
+      longest = rowMax;
+      bestD   = dMax;
+      bestE   = e;
+    }
+    const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
+    if (score > maxScore) {
+      maxScore = score;
+      msLen    = longest;
+      msD      = bestD;
+      msE      = bestE;
+    }
+
+    // Keep the band for the traceback.
+    const int cnt = R2 - L2 + 1;
+    if (used + cnt > w.cap.arenaCap) { w.err |= kErrArenaFull; return 0; }
+    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cur[d - Lc];
+    if (lane == 0) {
+      w.sc.rowOff[e] = used;
+      w.sc.rowL[e]   = L2;
+      w.sc.rowR[e]   = R2;
+    }
+    used += cnt;
+    int *t = prev;
+    prev   = cur;
+    cur    = t;
+    prevBase = Lc;
+    L        = L2;
+    R        = R2;
+    __syncwarp();
+  }
+
+  // Errors exhausted or every diagonal pruned (forward.C:306-313).
+  aEnd = STEP * msLen;
+  tEnd = STEP * (msLen + msD);
+  __syncwarp();
+  if (lane == 0) {
+    const int last = arena_get(w, msE, msD);
+    if (STEP > 0) set_right_delta(w, msE, msD, last);
+    else set_left_delta(w, msE, msD, last, leftover, tEnd, n);
+  }
+  if (STEP > 0) w.rightLen = __shfl_sync(0xffffffffu, w.rightLen, 0);
+  else {
+    w.leftLen = __shfl_sync(0xffffffffu, w.leftLen, 0);
+    leftover  = __shfl_sync(0xffffffffu, leftover, 0);
+    tEnd      = __shfl_sync(0xffffffffu, tEnd, 0);
+  }
+  toEnd = false;
+  __syncwarp();
+  return msE;
+}
+
+enum { kNone = 0, kLeftBranch = 1, kRightBranch = 2, kDovetail = 3 };
+
+// Extend_Alignment (prefixEditDistance-extend.C:36-183), one warp.  The merged delta
+// ends up in sc.deltaL[0 .. leftLen).  Outputs are warp-uniform.
+__device__ inline int warp_extend(WarpDP &w, const SeqView &S, int sLen, const SeqView &T, int tLen, int mStart,
+                           int mOffset, int mLen, int &sLo, int &sHi, int &tLo, int &tHi, int &errors) {
+  const int lane = threadIdx.x & 31;
+  int  rightErrors = 0, leftErrors = 0, leftover = 0;
+  bool rToEnd = true, lToEnd = true;
+  const int sLeftBegin = mStart - 1, sRightBegin = mStart + mLen, sRightLen = sLen - sRightBegin;
+  const int tLeftBegin = mOffset - 1, tRightBegin = mOffset + mLen, tRightLen = tLen - tRightBegin;
+  int totalOlap = min(mStart, mOffset) + mLen + min(sRightLen, tRightLen);
+  if (totalOlap < 0) totalOlap = 0;
+  if (totalOlap > (int)kMaxReadLen) totalOlap = (int)kMaxReadLen;
+  const int errorLimit = error_bound(totalOlap, w.P.maxErate);
+
+  w.leftLen = w.rightLen = 0;
+
+  if (sRightLen == 0 || tRightLen == 0) {
+    sHi = tHi = 0;
+    rToEnd    = true;
+  } else if (sRightLen <= tRightLen) {
+    rightErrors = warp_prefix_dp<+1>(w, S, sRightBegin, sRightLen, T, tRightBegin, tRightLen, errorLimit, sHi, tHi,
+                                     leftover, rToEnd);
+    if (w.err) return kNone;
+    for (int i = lane; i < w.rightLen; i += 32) w.sc.deltaR[i] = -w.sc.deltaR[i];
+  } else {
+    rightErrors = warp_prefix_dp<+1>(w, T, tRightBegin, tRightLen, S, sRightBegin, sRightLen, errorLimit, tHi, sHi,
+                                     leftover, rToEnd);
+    if (w.err) return kNone;
+  }
+  __syncwarp();
+  sHi += sRightBegin - 1;
+  tHi += tRightBegin - 1;
+
+  leftover = 0;
+  if (sLeftBegin < 0 || tLeftBegin < 0) {
+    sLo = tLo = 0;
+    lToEnd    = true;
+  } else if (sRightBegin <= tRightBegin) {
+    leftErrors = warp_prefix_dp<-1>(w, S, sLeftBegin, sLeftBegin + 1, T, tLeftBegin, tLeftBegin + 1,
+                                    errorLimit - rightErrors, sLo, tLo, leftover, lToEnd);
+    if (w.err) return kNone;
+  } else {
+    leftErrors = warp_prefix_dp<-1>(w, T, tLeftBegin, tLeftBegin + 1, S, sLeftBegin, sLeftBegin + 1,
+                                    errorLimit - rightErrors, tLo, sLo, leftover, lToEnd);
+    if (w.err) return kNone;
+    for (int i = lane; i < w.leftLen; i += 32) w.sc.deltaL[i] = -w.sc.deltaL[i];
+  }
+  __syncwarp();
+  sLo += sLeftBegin + 1;
+  tLo += tLeftBegin + 1;
+  errors = leftErrors + rightErrors;
+
+  const int kind = (!rToEnd) ? ((!lToEnd) ? kNone : kRightBranch) : ((!lToEnd) ? kLeftBranch : kDovetail);
+
+  // Merge the right delta into the left one (extend.C:164-175).
+  if (w.leftLen + w.rightLen + 1 > w.cap.rowCap) { w.err |= kErrDeltaFull; return kNone; }
+  if (w.rightLen > 0) {
+    const int base = w.leftLen;
+    if (lane == 0) {
+      const int r0 = w.sc.deltaR[0];
+      w.sc.deltaL[base] = (r0 > 0) ? -(r0 + leftover + mLen) : -(r0 - leftover - mLen);
+    }
+    for (int i = 1 + lane; i < w.rightLen; i += 32) w.sc.deltaL[base + i] = -w.sc.deltaR[i];
+    w.leftLen = base + w.rightLen;
+  }
+  w.rightLen = 0;
+  __syncwarp();
+  return kind;
+}
+
+}  // namespace oic

@@ -1,0 +1,1033 @@
+// oic_capi.cu -- the C ABI of liboic_gpu.so (include/oic_gpu.h): context, device
+// memory, host-side tables, and the orchestration of the kernels per hash block and
+// per batch of ref reads.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "oic_gpu.h"
+#include "oic_kernels.cuh"
+#include "oic_prims.cuh"
+
+using namespace oic;
+
+namespace {
+
+// ---------------------------------------------------------------------------------
+// Growable device buffer.
+struct DevBuf {
+  void  *p   = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+    size_t want = bytes ? bytes : 256;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p   = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return (T *)p; }
+};
+
+// Edit_Match_Limit: the minimum alignment length worth extending with e errors
+// (Binomial_Bound.C:36-97 and :104-195, AS_MAX_READLEN_BITS = 21), computed on the
+// host with the C library's pow/exp/sqrt like the reference.
+int binomial_bound(int e, double p, int start) {
+  const double q = 1.0 - p;
+  if (start < e) start = e;
+  for (int n = start; n < (int)kMaxReadLen; n++) {
+    if (n <= 35) {
+      double sum = 0.0, pPow = 1.0, qPow = pow(q, n);
+      int    coeff = 1, ct = 0;
+      for (int k = 0; k < e && 1.0 - sum > 1e-4; k++) {
+        sum += coeff * pPow * qPow;
+        coeff *= n - ct;
+        coeff /= ++ct;
+        pPow *= p;
+        qPow /= q;
+      }
+      if (1.0 - sum > 1e-4) return n;
+    } else {
+      const double z = (e - 0.5 - n * p) / sqrt(n * p * q);
+      if (z <= 3.62) return n;
+      double sum = 0.0, mu = 1.0, fact = 1.0;
+      const double pois = exp(-n * p);
+      for (int k = 0; k < e; k++) {
+        sum += mu * pois / fact;
+        mu *= n * p;
+        fact *= k + 1;
+      }
+      if (1.0 - sum > 1e-4) return n;
+    }
+  }
+  return (int)kMaxReadLen;
+}
+
+void match_limit(std::vector<int32_t> &ml, double erate, int32_t maxErrors) {
+  ml.assign((size_t)maxErrors + 1, 0);
+  int32_t e = 0, s = 1;
+  const int32_t l = std::min(maxErrors, 2000);
+  while (e <= 1) ml[e++] = 0;
+  while (e < l) {
+    s     = binomial_bound(e - 1, erate, s);
+    ml[e] = s - 1;
+    e++;
+  }
+  const double slope = 0.982064188397525 / erate + 0.067835741959926;
+  double v = ml[e - 1] + slope;
+  for (; e < maxErrors; e++) {
+    ml[e] = (int32_t)ceil(v);
+    v += slope;
+  }
+}
+
+int base2(char c) {
+  switch (c) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+    default: return -1;
+  }
+}
+
+}  // namespace
+
+struct oic_ctx {
+  oic_params   P;
+  DevParams    dp;
+  int          device = 0;
+  int          nSM    = 0;
+  cudaStream_t st     = nullptr;
+  std::string  lastErr;
+  std::vector<int32_t> eml;
+  DevBuf       dEml;
+
+  // reads
+  uint32_t              nReads = 0;
+  std::vector<uint32_t> len, lib;
+  std::vector<uint64_t> wordOff;
+  DevBuf dFwd, dRc, dNfwd, dNrc, dWordOff, dLen, dLib, dHasN;
+  ReadsDev R{};
+
+  // skip list
+  std::vector<uint64_t> skipKeys;
+  DevBuf                dSkip;
+
+  // hash block
+  bool     haveBlock = false;
+  uint32_t blkFirst = 0, blkN = 0;
+  uint64_t blkOcc = 0, blkDistinct = 0;
+  DevBuf dTKeys, dTVals, dOcc, dLscr, dRscr, dSlen, dSread;
+  DevBuf dSortK, dSortV, dSortK2, dSortV2, dFlags, dPos, dSortScratch, dStrRead, dStrKmers, dFlat, dNewKeys;
+  TableDev T{};
+
+  // seeds
+  DevBuf dSegReads, dPairs, dNodes, dSegOvf;
+  DevBuf dSeedSlotK, dSeedSlotV, dSeedPairs, dSeedNodes;        // normal configuration
+  DevBuf dSeedSlotK2, dSeedSlotV2, dSeedPairs2, dSeedNodes2;    // wide configuration
+  uint32_t pairCap = 0, nodeCap = 0;
+
+  // align
+  DevBuf dWork, dRec, dCnt, dRecPos, dRecOut, dAlnOvf;
+  DevBuf dArena, dRowOff, dRowL, dRowR, dDL, dDR, dStack, dAlive;           // normal
+  DevBuf dArena2, dRowOff2, dRowL2, dRowR2, dDL2, dDR2, dStack2, dAlive2;   // wide
+  DevBuf dScanScratch;
+
+  // counters (one small device block): [0..15] u32 counters, [16..] u64 stats
+  DevBuf dCtr;
+
+  std::vector<uint32_t> out;   // accumulated records, 6 words each
+  oic_stats stats{};
+};
+
+namespace {
+
+constexpr int kRetrySmaller = 100;   // run_batch: the batch's output did not fit
+
+enum CtrIdx {   // u32 counters
+  cSegCounter = 0, cPairCount, cNodeCount, cSegOvf, cWorkCounter, cAlnOvf, cErr, cRecTotal, cNumU32 = 16
+};
+constexpr int kSeedStatBase  = 16;   // u64 index: [seeds, segments]
+constexpr int kAlignStatBase = 20;   // u64 index: kStCount entries
+constexpr int kExtStatBase   = 40;
+
+uint32_t *ctr32(oic_ctx *c) { return c->dCtr.as<uint32_t>(); }
+unsigned long long *ctr64(oic_ctx *c) { return (unsigned long long *)c->dCtr.as<uint32_t>(); }
+
+int fail(oic_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->lastErr = buf;
+  if (getenv("OIC_VERBOSE")) fprintf(stderr, "oic: %s\n", buf);
+  return code;
+}
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? OIC_ERR_NOMEM : OIC_ERR_CUDA, "%s: %s", \
+                  #call, cudaGetErrorString(e_));                                              \
+  } while (0)
+
+bool verbose() { return getenv("OIC_VERBOSE") != nullptr; }
+
+uint32_t read_err(oic_ctx *ctx) {
+  uint32_t e = 0;
+  cudaMemcpyAsync(&e, ctr32(ctx) + cErr, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st);
+  cudaStreamSynchronize(ctx->st);
+  return e;
+}
+
+struct SeedConfig {
+  int warps;
+  SeedCaps caps;
+};
+
+SeedConfig seed_normal(const oic_ctx *c) {
+  SeedConfig s;
+  s.warps        = c->nSM * 8 * 4;
+  s.caps.slotCap = 4096;
+  s.caps.pairCap = 2048;
+  s.caps.nodeCap = 32768;
+  return s;
+}
+SeedConfig seed_wide(const oic_ctx *c) {
+  SeedConfig s;
+  s.warps        = c->nSM;
+  s.caps.slotCap = 1 << 17;
+  s.caps.pairCap = 1 << 16;
+  s.caps.nodeCap = 1 << 22;
+  return s;
+}
+
+int ensure_seed_scratch(oic_ctx *ctx, const SeedConfig &sc, bool wide, SeedScratch &out) {
+  DevBuf &k = wide ? ctx->dSeedSlotK2 : ctx->dSeedSlotK;
+  DevBuf &v = wide ? ctx->dSeedSlotV2 : ctx->dSeedSlotV;
+  DevBuf &p = wide ? ctx->dSeedPairs2 : ctx->dSeedPairs;
+  DevBuf &n = wide ? ctx->dSeedNodes2 : ctx->dSeedNodes;
+  const size_t W = (size_t)((sc.warps + 3) / 4 * 4);
+  CK(k.ensure(W * sc.caps.slotCap * sizeof(int)));
+  CK(v.ensure(W * sc.caps.slotCap * sizeof(int)));
+  CK(p.ensure(W * sc.caps.pairCap * sizeof(PairAcc)));
+  CK(n.ensure(W * sc.caps.nodeCap * sizeof(int4)));
+  out.slotKey = k.as<int>();
+  out.slotVal = v.as<int>();
+  out.pairs   = p.as<PairAcc>();
+  out.nodes   = n.as<int4>();
+  return OIC_OK;
+}
+
+struct AlignConfig {
+  int bandW;
+  int warps;
+  AlignCaps caps;
+};
+
+AlignConfig align_normal(const oic_ctx *c) {
+  AlignConfig a;
+  a.bandW         = 1024;
+  a.warps         = c->nSM * 3 * align_warps_per_block(1024);
+  a.caps.arenaCap = 1 << 19;
+  a.caps.rowCap   = 1 << 14;
+  a.caps.nodeCap  = 1 << 16;
+  a.caps.bandW    = 1024;
+  return a;
+}
+AlignConfig align_wide(const oic_ctx *c) {
+  AlignConfig a;
+  a.bandW         = 8192;
+  a.warps         = c->nSM;
+  a.caps.arenaCap = 1 << 24;
+  a.caps.rowCap   = 1 << 18;
+  a.caps.nodeCap  = 1 << 22;
+  a.caps.bandW    = 8192;
+  return a;
+}
+
+int ensure_align_scratch(oic_ctx *ctx, const AlignConfig &ac, bool wide, WarpScratch &s) {
+  const size_t W = (size_t)ac.warps;
+  DevBuf &ar = wide ? ctx->dArena2 : ctx->dArena;
+  DevBuf &ro = wide ? ctx->dRowOff2 : ctx->dRowOff;
+  DevBuf &rl = wide ? ctx->dRowL2 : ctx->dRowL;
+  DevBuf &rr = wide ? ctx->dRowR2 : ctx->dRowR;
+  DevBuf &dl = wide ? ctx->dDL2 : ctx->dDL;
+  DevBuf &dr = wide ? ctx->dDR2 : ctx->dDR;
+  DevBuf &sk = wide ? ctx->dStack2 : ctx->dStack;
+  DevBuf &al = wide ? ctx->dAlive2 : ctx->dAlive;
+  CK(ar.ensure(W * ac.caps.arenaCap * sizeof(int)));
+  CK(ro.ensure(W * ac.caps.rowCap * sizeof(int)));
+  CK(rl.ensure(W * ac.caps.rowCap * sizeof(int)));
+  CK(rr.ensure(W * ac.caps.rowCap * sizeof(int)));
+  CK(dl.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
+  CK(dr.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
+  CK(sk.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
+  CK(al.ensure(W * ac.caps.nodeCap));
+  s.arena  = ar.as<int>();
+  s.rowOff = ro.as<int>();
+  s.rowL   = rl.as<int>();
+  s.rowR   = rr.as<int>();
+  s.deltaL = dl.as<int>();
+  s.deltaR = dr.as<int>();
+  s.stack  = sk.as<int>();
+  s.alive  = al.as<unsigned char>();
+  return OIC_OK;
+}
+
+int sync_check(oic_ctx *ctx, const char *where) {
+  cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (e != cudaSuccess) return fail(ctx, OIC_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, OIC_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+  return OIC_OK;
+}
+
+// Process one batch of eligible ref reads against the loaded block.  Returns OIC_OK,
+// or OIC_ERR_OVERFLOW when the batch's output did not fit (caller splits the batch).
+int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
+              cudaEvent_t evAln1, float &msSeed, float &msAlign) {
+  const uint32_t nSeg = nRefs * 2;
+  CK(ctx->dSegReads.ensure((size_t)nRefs * sizeof(uint32_t)));
+  CK(cudaMemcpyAsync(ctx->dSegReads.p, refs, (size_t)nRefs * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctx->dCtr.p, 0, 64 * sizeof(uint32_t) + 0, ctx->st));
+  CK(cudaMemsetAsync(ctr64(ctx) + kSeedStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
+  CK(cudaMemsetAsync(ctr64(ctx) + kAlignStatBase, 0, kStCount * sizeof(unsigned long long), ctx->st));
+  CK(ctx->dSegOvf.ensure((size_t)nSeg * sizeof(uint32_t)));
+
+  SeedOut so;
+  so.pairs         = ctx->dPairs.as<PairRec>();
+  so.pairCap       = ctx->pairCap;
+  so.pairCount     = ctr32(ctx) + cPairCount;
+  so.nodes         = ctx->dNodes.as<int4>();
+  so.nodeCap       = ctx->nodeCap;
+  so.nodeCount     = ctr32(ctx) + cNodeCount;
+  so.overflowSegs  = ctx->dSegOvf.as<uint32_t>();
+  so.overflowCount = ctr32(ctx) + cSegOvf;
+  so.stats         = ctr64(ctx) + kSeedStatBase;
+  so.err           = ctr32(ctx) + cErr;
+
+  CK(cudaEventRecord(evSeed0, ctx->st));
+  SeedConfig sn = seed_normal(ctx);
+  SeedScratch ss;
+  int rc = ensure_seed_scratch(ctx, sn, false, ss);
+  if (rc) return rc;
+  launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), nSeg, ctr32(ctx) + cSegCounter, ss, sn.caps,
+              sn.warps, so, ctx->st);
+  uint32_t h[16];
+  CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "seed kernel"))) return rc;
+  if (h[cErr] & (kErrOutNodes | kErrOutPairs)) return kRetrySmaller;
+  if (h[cSegOvf] > 0) {
+    // Segments whose pair table or node pool overflowed: rerun them wide.
+    const uint32_t nOvf = h[cSegOvf];
+    std::vector<uint32_t> segs(nOvf), reads(nOvf);
+    CK(cudaMemcpyAsync(segs.data(), ctx->dSegOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    // A wide pass takes whole segments: encode each as its own (read, strand) pair.
+    std::vector<uint32_t> segReads2(nOvf);
+    for (uint32_t i = 0; i < nOvf; i++) segReads2[i] = refs[segs[i] >> 1];
+    DevBuf segBuf;
+    // Run strand by strand so that segment ids stay (read << 1 | strand).
+    SeedConfig sw = seed_wide(ctx);
+    SeedScratch ssw;
+    if ((rc = ensure_seed_scratch(ctx, sw, true, ssw))) return rc;
+    for (uint32_t i = 0; i < nOvf; i++) {
+      // one segment at a time through a 2-entry segment list: [read] with the strand picked by the id
+      uint32_t strand = segs[i] & 1;
+      uint32_t rd     = segReads2[i];
+      CK(segBuf.ensure(sizeof(uint32_t)));
+      CK(cudaMemcpyAsync(segBuf.p, &rd, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cSegCounter, 0, sizeof(uint32_t), ctx->st));
+      // nSeg = strand + 1 and counter pre-set to `strand` selects exactly segment `strand`.
+      uint32_t start = strand;
+      CK(cudaMemcpyAsync(ctr32(ctx) + cSegCounter, &start, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cSegOvf, 0, sizeof(uint32_t), ctx->st));
+      launch_seed(ctx->R, ctx->T, ctx->dp, segBuf.as<uint32_t>(), strand + 1, ctr32(ctx) + cSegCounter, ssw, sw.caps,
+                  sw.warps, so, ctx->st);
+      CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+      if ((rc = sync_check(ctx, "seed kernel (wide)"))) { segBuf.release(); return rc; }
+      if (h[cErr] & (kErrOutNodes | kErrOutPairs)) { segBuf.release(); return kRetrySmaller; }
+      if (h[cSegOvf] > 0) {
+        segBuf.release();
+        return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
+      }
+    }
+    segBuf.release();
+  }
+  CK(cudaEventRecord(evSeed1, ctx->st));
+  const uint32_t nPairs = h[cPairCount];
+  const uint32_t nNodes = h[cNodeCount];
+
+  // Align every pair.
+  CK(ctx->dWork.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
+  CK(ctx->dCnt.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
+  CK(ctx->dRecPos.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
+  CK(ctx->dRec.ensure((size_t)std::max<uint32_t>(nPairs, 1) * 18 * sizeof(uint32_t)));
+  CK(ctx->dAlnOvf.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
+  {
+    std::vector<uint32_t> work(nPairs);
+    for (uint32_t i = 0; i < nPairs; i++) work[i] = i;
+    if (nPairs) CK(cudaMemcpyAsync(ctx->dWork.p, work.data(), nPairs * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  if (nPairs) CK(cudaMemsetAsync(ctx->dCnt.p, 0, nPairs * sizeof(uint32_t), ctx->st));
+  AlignOut ao;
+  ao.rec           = ctx->dRec.as<uint32_t>();
+  ao.cnt           = ctx->dCnt.as<uint32_t>();
+  ao.overflow      = ctx->dAlnOvf.as<uint32_t>();
+  ao.overflowCount = ctr32(ctx) + cAlnOvf;
+  ao.stats         = ctr64(ctx) + kAlignStatBase;
+  ao.err           = ctr32(ctx) + cErr;
+  AlignConfig an = align_normal(ctx);
+  WarpScratch ws;
+  if ((rc = ensure_align_scratch(ctx, an, false, ws))) return rc;
+  launch_align(an.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
+               ctx->dWork.as<uint32_t>(), nPairs, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, an.caps,
+               an.warps, ao, ctx->st);
+  CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "align kernel"))) return rc;
+  if (h[cAlnOvf] > 0) {
+    const uint32_t nOvf = h[cAlnOvf];
+    if (verbose()) fprintf(stderr, "oic: %u pairs rerun in the wide DP configuration\n", nOvf);
+    // The overflow list becomes the work list of the wide configuration.
+    CK(cudaMemcpyAsync(ctx->dWork.p, ctx->dAlnOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cAlnOvf, 0, sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, sizeof(uint32_t), ctx->st));
+    AlignConfig aw = align_wide(ctx);
+    WarpScratch ww;
+    if ((rc = ensure_align_scratch(ctx, aw, true, ww))) return rc;
+    launch_align(aw.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
+                 ctx->dWork.as<uint32_t>(), nOvf, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ww, aw.caps,
+                 aw.warps, ao, ctx->st);
+    CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = sync_check(ctx, "align kernel (wide)"))) return rc;
+    if (h[cAlnOvf] > 0)
+      return fail(ctx, OIC_ERR_OVERFLOW, "a read pair needs a wider DP band or deeper traceback than the engine holds (err 0x%x)",
+                  h[cErr]);
+  }
+  CK(cudaEventRecord(evAln1, ctx->st));
+
+  // Compact the records and bring them home.
+  CK(ctx->dScanScratch.ensure(scan_u32_scratch(nPairs) + 256));
+  CK(scan_u32(ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), nPairs, ctr32(ctx) + cRecTotal,
+              ctx->dScanScratch.p, ctx->st));
+  uint32_t nRec = 0;
+  CK(cudaMemcpyAsync(&nRec, ctr32(ctx) + cRecTotal, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (nRec) {
+    CK(ctx->dRecOut.ensure((size_t)nRec * 6 * sizeof(uint32_t)));
+    launch_compact_records(ctx->dRec.as<uint32_t>(), ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), nPairs,
+                           ctx->dRecOut.as<uint32_t>(), ctx->st);
+    size_t old = ctx->out.size();
+    ctx->out.resize(old + (size_t)nRec * 6);
+    CK(cudaMemcpyAsync(ctx->out.data() + old, ctx->dRecOut.p, (size_t)nRec * 6 * sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  }
+  unsigned long long st64[2 + kStCount];
+  CK(cudaMemcpyAsync(st64, ctr64(ctx) + kSeedStatBase, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(st64 + 2, ctr64(ctx) + kAlignStatBase, kStCount * sizeof(unsigned long long),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "record compaction"))) return rc;
+
+  float a = 0, b = 0;
+  cudaEventElapsedTime(&a, evSeed0, evSeed1);
+  cudaEventElapsedTime(&b, evSeed1, evAln1);
+  msSeed += a;
+  msAlign += b;
+
+  oic_stats &S = ctx->stats;
+  S.seeds += st64[0];
+  S.candidatePairs += nPairs;
+  S.nodes += nNodes;
+  S.kmerHitsWithoutOlap += st64[2 + kStWithoutOlap];
+  S.kmerHitsWithOlap += st64[2 + kStWithOlap];
+  S.kmerHitsSkipped += st64[2 + kStSkipped];
+  S.multiOverlap += st64[2 + kStMulti];
+  S.totalOverlaps += st64[2 + kStTotal];
+  S.containedOverlaps += st64[2 + kStContained];
+  S.dovetailOverlaps += st64[2 + kStDovetail];
+  S.dpCells += st64[2 + kStCells];
+  S.slideBases += st64[2 + kStSlides];
+  S.extensions += st64[2 + kStExtensions];
+  return OIC_OK;
+}
+
+}  // namespace
+
+// =================================================================================
+extern "C" {
+
+void oic_default_params(oic_params *p) {
+  memset(p, 0, sizeof(*p));
+  p->maxErate          = 0.06;
+  p->alignNoise        = 1.0;
+  p->uniqueOlapPerPair = 1;
+  p->useHopelessCheck  = 1;
+  p->hashBits          = 22;
+  p->maxHashLoad       = 0.6;
+  p->maxHashDataLen    = 100000000;
+  p->numThreads        = 1;
+  p->bgnHashID         = 1;
+  p->endHashID         = UINT32_MAX;
+  p->maxLibToHash      = UINT32_MAX;
+  p->bgnRefID          = 1;
+  p->endRefID          = UINT32_MAX;
+  p->maxLibToRef       = UINT32_MAX;
+}
+
+int oic_create(const oic_params *p, int device, oic_ctx **out) {
+  if (!p || !out) return OIC_ERR_ARG;
+  *out = nullptr;
+  if (p->kmerLen < 1 || p->kmerLen > 31) return OIC_ERR_ARG;
+  if (p->hashBits < 1 || p->hashBits > 40) return OIC_ERR_ARG;
+  if (!(p->maxErate > 0.0) || p->maxErate > 0.65) return OIC_ERR_ARG;
+  if (!(p->alignNoise > 0.0)) return OIC_ERR_ARG;
+
+  oic_ctx *ctx = new oic_ctx();
+  ctx->P = *p;
+  if (ctx->P.maxErate > 0.06) ctx->P.useHopelessCheck = 0;   // overlapInCore.C:400-401
+  if (ctx->P.numThreads < 1) ctx->P.numThreads = 1;
+
+  int nDev = 0;
+  cudaError_t e = cudaGetDeviceCount(&nDev);
+  if (e != cudaSuccess || device < 0 || device >= nDev) {
+    int code = fail(ctx, OIC_ERR_CUDA, "no usable CUDA device %d (%s)", device,
+                    e == cudaSuccess ? "not present" : cudaGetErrorString(e));
+    delete ctx;
+    return code;
+  }
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking)) !=
+                                                         cudaSuccess) {
+    delete ctx;
+    return OIC_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->nSM, cudaDevAttrMultiProcessorCount, device);
+  if (ctx->nSM <= 0) ctx->nSM = 1;
+
+  // prefixEditDistance constructor (prefixEditDistance.C:23-90).
+  const double erate     = ctx->P.maxErate;
+  const int32_t maxErrors = 1 + (int32_t)ceil(erate * (double)kMaxReadLen);
+  match_limit(ctx->eml, erate * ctx->P.alignNoise, maxErrors);
+  DevParams &dp        = ctx->dp;
+  dp.maxErate          = erate;
+  dp.branchMatchValue  = erate / (1 + erate);
+  dp.minBranchTailSlope = (erate > 0.06) ? 1.0 : 0.20;
+  dp.kmerExpect        = exp(-1.0 * (double)ctx->P.kmerLen * erate);
+  dp.minKmers          = 0;
+  if (ctx->P.minKmers)   // overlapInCore.C:410-411
+    dp.minKmers = (unsigned long long)(int)floor(
+        dp.kmerExpect * (double)((uint64_t)(int64_t)ctx->P.minOlapLen - (uint64_t)ctx->P.kmerLen + 1));
+  dp.kmerLen    = (int)ctx->P.kmerLen;
+  dp.partial    = ctx->P.partial ? 1 : 0;
+  dp.unique     = ctx->P.uniqueOlapPerPair ? 1 : 0;
+  dp.hopeless   = ctx->P.useHopelessCheck ? 1 : 0;
+  dp.minOlapLen = ctx->P.minOlapLen;
+  dp.maxErrors  = maxErrors;
+
+  int rc = OIC_OK;
+  if ((e = ctx->dEml.ensure(ctx->eml.size() * sizeof(int32_t))) != cudaSuccess ||
+      (e = cudaMemcpy(ctx->dEml.p, ctx->eml.data(), ctx->eml.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
+          cudaSuccess ||
+      (e = ctx->dCtr.ensure(4096)) != cudaSuccess) {
+    rc = OIC_ERR_CUDA;
+  }
+  if (rc) {
+    oic_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return OIC_OK;
+}
+
+void oic_destroy(oic_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  DevBuf *bufs[] = {&ctx->dEml,      &ctx->dFwd,        &ctx->dRc,         &ctx->dNfwd,      &ctx->dNrc,
+                    &ctx->dWordOff,  &ctx->dLen,        &ctx->dLib,        &ctx->dHasN,      &ctx->dSkip,
+                    &ctx->dTKeys,    &ctx->dTVals,      &ctx->dOcc,        &ctx->dLscr,      &ctx->dRscr,
+                    &ctx->dSlen,     &ctx->dSread,      &ctx->dSortK,      &ctx->dSortV,     &ctx->dSortK2,
+                    &ctx->dSortV2,   &ctx->dFlags,      &ctx->dPos,        &ctx->dSortScratch, &ctx->dStrRead,
+                    &ctx->dStrKmers, &ctx->dFlat,       &ctx->dNewKeys,    &ctx->dSegReads,  &ctx->dPairs,
+                    &ctx->dNodes,    &ctx->dSegOvf,     &ctx->dSeedSlotK,  &ctx->dSeedSlotV, &ctx->dSeedPairs,
+                    &ctx->dSeedNodes, &ctx->dSeedSlotK2, &ctx->dSeedSlotV2, &ctx->dSeedPairs2, &ctx->dSeedNodes2,
+                    &ctx->dWork,     &ctx->dRec,        &ctx->dCnt,        &ctx->dRecPos,    &ctx->dRecOut,
+                    &ctx->dAlnOvf,   &ctx->dArena,      &ctx->dRowOff,     &ctx->dRowL,      &ctx->dRowR,
+                    &ctx->dDL,       &ctx->dDR,         &ctx->dStack,      &ctx->dAlive,     &ctx->dArena2,
+                    &ctx->dRowOff2,  &ctx->dRowL2,      &ctx->dRowR2,      &ctx->dDL2,       &ctx->dDR2,
+                    &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr};
+  for (DevBuf *b : bufs) b->release();
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+const char *oic_last_error(oic_ctx *ctx) { return ctx ? ctx->lastErr.c_str() : "no context"; }
+
+int oic_get_match_limit(oic_ctx *ctx, int32_t *dst, uint32_t n, uint32_t *len) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (len) *len = (uint32_t)ctx->eml.size();
+  if (dst) memcpy(dst, ctx->eml.data(), sizeof(int32_t) * std::min<size_t>(n, ctx->eml.size()));
+  return OIC_OK;
+}
+
+int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const uint32_t *length,
+                  const uint64_t *offset, const char *bases, uint64_t nBases) {
+  if (!ctx || (nReads && (!length || !offset || !bases))) return OIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  ctx->haveBlock = false;
+  ctx->nReads    = nReads;
+  ctx->len.assign(length, length + nReads);
+  ctx->lib.resize(nReads);
+  for (uint32_t i = 0; i < nReads; i++) ctx->lib[i] = libID ? libID[i] : 1;
+  ctx->wordOff.resize((size_t)nReads + 1);
+  uint64_t w = 1;
+  for (uint32_t i = 0; i < nReads; i++) {
+    if (length[i] > kMaxReadLen) return fail(ctx, OIC_ERR_INPUT, "read %u is longer than %u bases", i + 1, kMaxReadLen);
+    if (offset[i] + length[i] > nBases) return fail(ctx, OIC_ERR_ARG, "read %u lies outside the base buffer", i + 1);
+    ctx->wordOff[i] = w;
+    w += (length[i] + 31) / 32 + 1;
+  }
+  ctx->wordOff[nReads] = w;
+  const uint64_t nWords = w + 2;
+
+  CK(ctx->dFwd.ensure(nWords * 8));
+  CK(ctx->dRc.ensure(nWords * 8));
+  CK(ctx->dNfwd.ensure(nWords * 8));
+  CK(ctx->dNrc.ensure(nWords * 8));
+  CK(cudaMemsetAsync(ctx->dFwd.p, 0, nWords * 8, ctx->st));
+  CK(cudaMemsetAsync(ctx->dRc.p, 0, nWords * 8, ctx->st));
+  CK(cudaMemsetAsync(ctx->dNfwd.p, 0, nWords * 8, ctx->st));
+  CK(cudaMemsetAsync(ctx->dNrc.p, 0, nWords * 8, ctx->st));
+  CK(ctx->dWordOff.ensure((size_t)(nReads + 1) * 8));
+  CK(ctx->dLen.ensure((size_t)(nReads + 1) * 4));
+  CK(ctx->dLib.ensure((size_t)(nReads + 1) * 4));
+  CK(ctx->dHasN.ensure((size_t)(nReads + 1)));
+  if (nReads) {
+    CK(cudaMemcpyAsync(ctx->dWordOff.p, ctx->wordOff.data(), (size_t)nReads * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->dLen.p, length, (size_t)nReads * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->dLib.p, ctx->lib.data(), (size_t)nReads * 4, cudaMemcpyHostToDevice, ctx->st));
+    DevBuf ascii, off;
+    CK(ascii.ensure(nBases + 64));
+    CK(off.ensure((size_t)nReads * 8));
+    CK(cudaMemcpyAsync(ascii.p, bases, nBases, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(off.p, offset, (size_t)nReads * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, 4, ctx->st));
+    launch_pack_reads(ascii.as<char>(), off.as<u64>(), ctx->dLen.as<uint32_t>(), ctx->dWordOff.as<u64>(),
+                      nReads, ctx->dFwd.as<u64>(), ctx->dRc.as<u64>(), ctx->dNfwd.as<u64>(), ctx->dNrc.as<u64>(),
+                      ctx->dHasN.as<unsigned char>(), ctr32(ctx) + cErr, ctx->st);
+    int rc = sync_check(ctx, "pack reads");
+    uint32_t err = read_err(ctx);
+    ascii.release();
+    off.release();
+    if (rc) return rc;
+    if (err & kErrBadBase) return fail(ctx, OIC_ERR_INPUT, "a read holds a character other than A, C, G, T or N");
+  }
+  ReadsDev &R = ctx->R;
+  R.fwd     = ctx->dFwd.as<u64>();
+  R.rc      = ctx->dRc.as<u64>();
+  R.nfwd    = ctx->dNfwd.as<u64>();
+  R.nrc     = ctx->dNrc.as<u64>();
+  R.wordOff = ctx->dWordOff.as<u64>();
+  R.len     = ctx->dLen.as<uint32_t>();
+  R.lib     = ctx->dLib.as<uint32_t>();
+  R.hasN    = ctx->dHasN.as<unsigned char>();
+  R.nReads  = nReads;
+  return OIC_OK;
+}
+
+int oic_set_skip_kmers(oic_ctx *ctx, const char *kmers, uint64_t nKmers) {
+  if (!ctx || (nKmers && !kmers)) return OIC_ERR_ARG;
+  const uint32_t K = ctx->P.kmerLen;
+  ctx->skipKeys.clear();
+  ctx->skipKeys.reserve(nKmers * 2);
+  for (uint64_t i = 0; i < nKmers; i++) {
+    const char *s = kmers + i * K;
+    uint64_t fw = 0, rc = 0;
+    for (uint32_t j = 0; j < K; j++) {
+      int c = base2(s[j]);
+      if (c < 0) return fail(ctx, OIC_ERR_INPUT, "skip k-mer %lu is not ACGT", (unsigned long)(i + 1));
+      fw |= (uint64_t)c << (2 * j);                // Mark_Skip_Kmers, Build_Hash_Index.C:231-232
+      rc |= (uint64_t)(3 - c) << (2 * (K - 1 - j));
+    }
+    ctx->skipKeys.push_back(fw);
+    ctx->skipKeys.push_back(rc);
+  }
+  return OIC_OK;
+}
+
+int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *lastLoaded) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (ctx->nReads == 0) return fail(ctx, OIC_ERR_STATE, "no reads loaded");
+  cudaSetDevice(ctx->device);
+  if (bgnID < 1) bgnID = 1;
+  if (endID > ctx->nReads) endID = ctx->nReads;
+  if (bgnID > endID) return fail(ctx, OIC_ERR_ARG, "empty hash range %u-%u", bgnID, endID);
+  const oic_params &P = ctx->P;
+  const uint32_t K = P.kmerLen;
+  const uint64_t maxData  = P.maxHashDataLen + kMaxReadLen;                        // overlapInCore.C:454
+  const uint64_t tableSz  = (uint64_t)1 << P.hashBits;
+  const uint64_t entryLim = (uint64_t)(P.maxHashLoad * (double)tableSz * kEntriesPerBucket);   // :445
+
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev0, ctx->st);
+
+  // Candidate strings under the data-length limit (Build_Hash_Index.C:504-545).
+  std::vector<uint32_t> strRead, strKmers, strLen;
+  std::vector<uint64_t> flat(1, 0);
+  std::vector<uint8_t>  eligible;
+  uint64_t total = 0;
+  for (uint32_t cur = bgnID; total < maxData && cur <= endID; cur++) {
+    const uint32_t r  = cur - 1;
+    const bool     ok = ctx->lib[r] >= P.minLibToHash && ctx->lib[r] <= P.maxLibToHash &&
+                    (int64_t)ctx->len[r] >= (int64_t)P.minOlapLen;
+    if (ok && ctx->len[r] < K) return fail(ctx, OIC_ERR_INPUT, "read %u is shorter than the k-mer size", cur);
+    strRead.push_back(r);
+    eligible.push_back(ok ? 1 : 0);
+    strLen.push_back(ok ? ctx->len[r] : 0);
+    const uint32_t nk = ok ? ctx->len[r] - K + 1 : 0;
+    strKmers.push_back(nk);
+    flat.push_back(flat.back() + nk);
+    if (ok) total += (uint64_t)ctx->len[r] + 1;
+  }
+  const uint32_t nCand = (uint32_t)strRead.size();
+  const uint64_t nFlat = flat.back();
+  if (nFlat >= 0xffffffffull) return fail(ctx, OIC_ERR_OVERFLOW, "hash block holds more than 2^32 k-mers");
+
+  CK(ctx->dStrRead.ensure((size_t)nCand * 4 + 4));
+  CK(ctx->dStrKmers.ensure((size_t)nCand * 4 + 4));
+  CK(ctx->dFlat.ensure((size_t)(nCand + 1) * 8));
+  CK(ctx->dNewKeys.ensure((size_t)nCand * 4 + 4));
+  CK(cudaMemcpyAsync(ctx->dStrRead.p, strRead.data(), nCand * 4, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->dStrKmers.p, strKmers.data(), nCand * 4, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->dFlat.p, flat.data(), (size_t)(nCand + 1) * 8, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctx->dNewKeys.p, 0, (size_t)nCand * 4 + 4, ctx->st));
+
+  const size_t n = (size_t)nFlat;
+  CK(ctx->dSortK.ensure(n * 8 + 8));
+  CK(ctx->dSortV.ensure(n * 4 + 4));
+  CK(ctx->dSortK2.ensure(n * 8 + 8));
+  CK(ctx->dSortV2.ensure(n * 4 + 4));
+  CK(ctx->dFlags.ensure(n * 4 + 4));
+  CK(ctx->dPos.ensure(n * 4 + 4));
+  CK(ctx->dSortScratch.ensure(std::max(radix_sort_scratch(n), scan_u32_scratch(n)) + 256));
+
+  launch_kmer_emit(ctx->R, ctx->dStrRead.as<uint32_t>(), ctx->dStrKmers.as<uint32_t>(), ctx->dFlat.as<u64>(), nCand,
+                   (int)K, ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), ctx->st);
+  CK(radix_sort_u64_u32(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), ctx->dSortK2.as<u64>(),
+                        ctx->dSortV2.as<uint32_t>(), n, 2 * (int)K + 1, ctx->dSortScratch.p, ctx->st));
+  launch_first_occ(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), n, ctx->dFlat.as<u64>(), nCand, (int)K,
+                   ctx->dNewKeys.as<uint32_t>(), ctx->st);
+  std::vector<uint32_t> newKeys(nCand);
+  CK(cudaMemcpyAsync(newKeys.data(), ctx->dNewKeys.p, (size_t)nCand * 4, cudaMemcpyDeviceToHost, ctx->st));
+  int rc = sync_check(ctx, "hash k-mer sort");
+  if (rc) return rc;
+
+  // The load loop stops before a read once the data length or the distinct-k-mer
+  // count reached its limit (Build_Hash_Index.C:504-506).
+  uint32_t cut = 0;
+  uint64_t len = 0, distinct = 0;
+  for (; cut < nCand; cut++) {
+    if (!(len < maxData && distinct < entryLim)) break;
+    if (eligible[cut]) len += (uint64_t)strLen[cut] + 1;
+    distinct += newKeys[cut];
+  }
+  const uint32_t nStr = cut;
+
+  // Keep the occurrences of the loaded strings (and drop windows with an N).
+  launch_keep_flags(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), n, (int)K, (uint32_t)flat[nStr],
+                    ctx->dFlags.as<uint32_t>(), ctx->st);
+  CK(scan_u32(ctx->dFlags.as<uint32_t>(), ctx->dPos.as<uint32_t>(), n, ctr32(ctx) + cRecTotal, ctx->dSortScratch.p,
+              ctx->st));
+  launch_compact_kv(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), ctx->dFlags.as<uint32_t>(),
+                    ctx->dPos.as<uint32_t>(), n, ctx->dSortK2.as<u64>(), ctx->dSortV2.as<uint32_t>(), ctx->st);
+  uint32_t nOcc = 0;
+  CK(cudaMemcpyAsync(&nOcc, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "hash compaction"))) return rc;
+
+  uint64_t cap = 1024;
+  while (cap < 2 * (distinct + ctx->skipKeys.size() + 1)) cap <<= 1;
+  CK(ctx->dTKeys.ensure(cap * 8));
+  CK(ctx->dTVals.ensure(cap * 8));
+  CK(ctx->dOcc.ensure((size_t)nOcc * 8 + 8));
+  CK(cudaMemsetAsync(ctx->dTKeys.p, 0xff, cap * 8, ctx->st));
+  CK(cudaMemsetAsync(ctx->dTVals.p, 0, cap * 8, ctx->st));
+  CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, 4, ctx->st));
+  launch_table_build(ctx->dSortK2.as<u64>(), nOcc, ctx->dTKeys.as<u64>(), ctx->dTVals.as<u64>(), cap - 1,
+                     ctr32(ctx) + cErr, ctx->st);
+  launch_occ_convert(ctx->dSortV2.as<uint32_t>(), nOcc, ctx->dFlat.as<u64>(), std::max<uint32_t>(nStr, 1),
+                     ctx->dOcc.as<u64>(), ctx->st);
+
+  // String_Info (Build_Hash_Index.C:511-536): loaded strings unscreened, skipped ones screened.
+  std::vector<uint8_t>  lscr(nStr), rscr(nStr);
+  std::vector<uint32_t> slen(nStr), sread(nStr);
+  for (uint32_t s = 0; s < nStr; s++) {
+    lscr[s] = rscr[s] = eligible[s] ? 0 : 1;
+    slen[s]  = strLen[s];
+    sread[s] = strRead[s];
+  }
+  CK(ctx->dLscr.ensure(nStr + 1));
+  CK(ctx->dRscr.ensure(nStr + 1));
+  CK(ctx->dSlen.ensure((size_t)nStr * 4 + 4));
+  CK(ctx->dSread.ensure((size_t)nStr * 4 + 4));
+  CK(cudaMemcpyAsync(ctx->dLscr.p, lscr.data(), nStr, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->dRscr.p, rscr.data(), nStr, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->dSlen.p, slen.data(), (size_t)nStr * 4, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->dSread.p, sread.data(), (size_t)nStr * 4, cudaMemcpyHostToDevice, ctx->st));
+
+  TableDev &T = ctx->T;
+  T.keys     = ctx->dTKeys.as<u64>();
+  T.vals     = ctx->dTVals.as<u64>();
+  T.mask     = cap - 1;
+  T.occ      = ctx->dOcc.as<u64>();
+  T.lscr     = ctx->dLscr.as<unsigned char>();
+  T.rscr     = ctx->dRscr.as<unsigned char>();
+  T.slen     = ctx->dSlen.as<uint32_t>();
+  T.sread    = ctx->dSread.as<uint32_t>();
+  T.firstID  = bgnID;
+  T.nStrings = nStr;
+
+  if (!ctx->skipKeys.empty()) {
+    CK(ctx->dSkip.ensure(ctx->skipKeys.size() * 8));
+    CK(cudaMemcpyAsync(ctx->dSkip.p, ctx->skipKeys.data(), ctx->skipKeys.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    launch_skip_mark(ctx->dSkip.as<u64>(), ctx->skipKeys.size(), T, ctx->dTKeys.as<u64>(), ctx->dTVals.as<u64>(),
+                     ctx->dLscr.as<unsigned char>(), ctx->dRscr.as<unsigned char>(), (int)K, P.useHopelessCheck ? 1 : 0,
+                     ctr32(ctx) + cErr, ctx->st);
+  }
+  cudaEventRecord(ev1, ctx->st);
+  if ((rc = sync_check(ctx, "hash table build"))) return rc;
+  uint32_t err = read_err(ctx);
+  if (err & kErrTableFull) return fail(ctx, OIC_ERR_DEVICE, "k-mer table full");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  ctx->stats.msHash += ms;
+  ctx->stats.nHashBlocks++;
+
+  ctx->haveBlock   = true;
+  ctx->blkFirst    = bgnID;
+  ctx->blkN        = nStr;
+  ctx->blkOcc      = nOcc;
+  ctx->blkDistinct = distinct;
+  if (verbose())
+    fprintf(stderr, "oic: hash block %u-%u: %u strings, %lu distinct k-mers, %u occurrences, %.2f ms\n", bgnID,
+            bgnID + nStr - 1, nStr, (unsigned long)distinct, nOcc, ms);
+  if (lastLoaded) *lastLoaded = bgnID + nStr - 1;
+  return OIC_OK;
+}
+
+int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (!ctx->haveBlock) return fail(ctx, OIC_ERR_STATE, "no hash block loaded");
+  cudaSetDevice(ctx->device);
+  const oic_params &P = ctx->P;
+  if (bgnRefID < 1) bgnRefID = 1;
+  if (endRefID > ctx->nReads) endRefID = ctx->nReads;
+  std::vector<uint32_t> refs;
+  for (uint64_t id = bgnRefID; id <= endRefID; id++) {
+    const uint32_t r = (uint32_t)id - 1;
+    if (ctx->lib[r] < P.minLibToRef || ctx->lib[r] > P.maxLibToRef) continue;     // Process_Overlaps.C:50-55
+    if ((int64_t)ctx->len[r] < (int64_t)P.minOlapLen) continue;
+    if (ctx->len[r] < P.kmerLen) return fail(ctx, OIC_ERR_INPUT, "read %u is shorter than the k-mer size", (uint32_t)id);
+    refs.push_back(r);
+  }
+  if (refs.empty()) return OIC_OK;
+
+  // Output capacities for a batch.
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  if (ctx->pairCap == 0) {
+    ctx->pairCap = 8u << 20;
+    ctx->nodeCap = 256u << 20;
+    if (freeB < ((size_t)48 << 30)) {
+      ctx->pairCap = 2u << 20;
+      ctx->nodeCap = 32u << 20;
+    }
+    CK(ctx->dPairs.ensure((size_t)ctx->pairCap * sizeof(PairRec)));
+    CK(ctx->dNodes.ensure((size_t)ctx->nodeCap * sizeof(int4)));
+  }
+
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  float msSeed = 0, msAlign = 0;
+  size_t   pos   = 0;
+  uint32_t batch = (uint32_t)refs.size();
+  int      rc    = OIC_OK;
+  while (pos < refs.size()) {
+    const uint32_t nb = (uint32_t)std::min<size_t>(batch, refs.size() - pos);
+    const size_t   outMark = ctx->out.size();
+    const oic_stats saved  = ctx->stats;
+    rc = run_batch(ctx, refs.data() + pos, nb, e0, e1, e2, msSeed, msAlign);
+    if (rc == kRetrySmaller && nb > 1) {
+      ctx->out.resize(outMark);
+      ctx->stats = saved;
+      batch      = (nb + 1) / 2;
+      if (verbose()) fprintf(stderr, "oic: batch output full, retrying with %u ref reads per batch\n", batch);
+      continue;
+    }
+    if (rc) break;
+    pos += nb;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  ctx->stats.msSeed += msSeed;
+  ctx->stats.msAlign += msAlign;
+  if (rc == kRetrySmaller) return fail(ctx, OIC_ERR_OVERFLOW, "a single ref read's output does not fit");
+  return rc;
+}
+
+int oic_run(oic_ctx *ctx) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (ctx->nReads == 0) return fail(ctx, OIC_ERR_STATE, "no reads loaded");
+  oic_params G = ctx->P;
+  const uint32_t last = ctx->nReads;
+  // OverlapDriver range clamping (overlapInCore.C:179-189).
+  if (G.bgnHashID < 1) G.bgnHashID = 1;
+  if (last < G.endHashID) G.endHashID = last;
+  if (G.bgnRefID < 1) G.bgnRefID = 1;
+  if (G.endRefID > last) G.endRefID = last;
+
+  // Every read the reference visits must be at least k long (Find_Overlaps.C:249).
+  for (uint32_t r = 0; r < last; r++)
+    if ((int64_t)ctx->len[r] >= (int64_t)G.minOlapLen && ctx->len[r] < G.kmerLen)
+      return fail(ctx, OIC_ERR_INPUT, "read %u is shorter than the k-mer size", r + 1);
+
+  // Thread chunks start at bgnRef + k * perThread and a chunk starting on endRef is
+  // never run (Process_Overlaps.C:33, overlapInCore.C:225).
+  uint32_t refEnd = G.endRefID;
+  bool     anyRef = G.bgnRefID < G.endRefID;
+  if (G.bgnRefID <= G.endRefID) {
+    const uint32_t perThread = 1 + (G.endRefID - G.bgnRefID) / G.numThreads / 8;
+    if ((G.endRefID - G.bgnRefID) % perThread == 0) refEnd = G.endRefID - 1;
+  }
+
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, ctx->st);
+  int rc = OIC_OK;
+  uint32_t bgnH = G.bgnHashID;
+  while (bgnH < G.endHashID) {   // overlapInCore.C:204
+    uint32_t lastLoaded = 0;
+    if ((rc = oic_load_hash_block(ctx, bgnH, G.endHashID, &lastLoaded))) break;
+    if (anyRef && (rc = oic_run_refs(ctx, G.bgnRefID, refEnd))) break;
+    bgnH = lastLoaded + 1;
+  }
+  cudaEventRecord(t1, ctx->st);
+  cudaEventSynchronize(t1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, t0, t1);
+  ctx->stats.msTotal += ms;
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  return rc;
+}
+
+int oic_num_overlaps(oic_ctx *ctx, uint64_t *n) {
+  if (!ctx || !n) return OIC_ERR_ARG;
+  *n = ctx->out.size() / 6;
+  return OIC_OK;
+}
+
+int oic_fetch_overlaps(oic_ctx *ctx, uint32_t *words, uint64_t maxRecords, uint64_t *n) {
+  if (!ctx || (!words && maxRecords)) return OIC_ERR_ARG;
+  const uint64_t have = ctx->out.size() / 6, k = std::min(have, maxRecords);
+  if (k) memcpy(words, ctx->out.data(), (size_t)k * 6 * sizeof(uint32_t));
+  if (n) *n = k;
+  return OIC_OK;
+}
+
+int oic_clear_overlaps(oic_ctx *ctx) {
+  if (!ctx) return OIC_ERR_ARG;
+  ctx->out.clear();
+  ctx->stats = oic_stats{};
+  return OIC_OK;
+}
+
+int oic_get_stats(oic_ctx *ctx, oic_stats *st) {
+  if (!ctx || !st) return OIC_ERR_ARG;
+  *st = ctx->stats;
+  return OIC_OK;
+}
+
+int oic_extend_batch(oic_ctx *ctx, uint32_t nAlign, const uint32_t *sRead, const uint32_t *sRev,
+                     const uint32_t *tRead, const int32_t *mStart, const int32_t *mOffset, const int32_t *mLen,
+                     int32_t *out, int32_t *kind, int32_t *deltaLen) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (nAlign == 0) return OIC_OK;
+  if (!sRead || !sRev || !tRead || !mStart || !mOffset || !mLen || !out || !kind || !deltaLen) return OIC_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<ExtendProblem> pb(nAlign);
+  for (uint32_t i = 0; i < nAlign; i++) {
+    if (sRead[i] < 1 || sRead[i] > ctx->nReads || tRead[i] < 1 || tRead[i] > ctx->nReads)
+      return fail(ctx, OIC_ERR_ARG, "problem %u names a read outside the store", i);
+    const int sl = (int)ctx->len[sRead[i] - 1], tl = (int)ctx->len[tRead[i] - 1];
+    if (mLen[i] < 1 || mStart[i] < 0 || mOffset[i] < 0 || mStart[i] + mLen[i] > sl || mOffset[i] + mLen[i] > tl)
+      return fail(ctx, OIC_ERR_ARG, "problem %u: match outside the reads", i);
+    pb[i] = ExtendProblem{sRead[i] - 1, sRev[i] ? 1u : 0u, tRead[i] - 1, mStart[i], mOffset[i], mLen[i]};
+  }
+  DevBuf dP, dOut, dKind, dDl, dStatus;
+  CK(dP.ensure(nAlign * sizeof(ExtendProblem)));
+  CK(dOut.ensure((size_t)nAlign * 5 * 4));
+  CK(dKind.ensure((size_t)nAlign * 4));
+  CK(dDl.ensure((size_t)nAlign * 4));
+  CK(dStatus.ensure((size_t)nAlign * 4));
+  CK(cudaMemcpyAsync(dP.p, pb.data(), nAlign * sizeof(ExtendProblem), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctr64(ctx) + kExtStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
+  std::vector<uint32_t> status(nAlign);
+  int rc = OIC_OK;
+  for (int pass = 0; pass < 2 && rc == OIC_OK; pass++) {
+    CK(cudaMemsetAsync(ctr64(ctx) + kExtStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
+    AlignConfig ac = pass == 0 ? align_normal(ctx) : align_wide(ctx);
+    WarpScratch ws;
+    if ((rc = ensure_align_scratch(ctx, ac, pass == 1, ws))) break;
+    launch_extend_batch(ac.bandW, ctx->R, ctx->dp, ctx->dEml.as<int>(), dP.as<ExtendProblem>(), nAlign, ws, ac.caps,
+                        ac.warps, dOut.as<int>(), dKind.as<int>(), dDl.as<int>(), dStatus.as<uint32_t>(),
+                        ctr64(ctx) + kExtStatBase, ctx->st);
+    CK(cudaMemcpyAsync(status.data(), dStatus.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = sync_check(ctx, "extend batch"))) break;
+    bool any = false;
+    for (uint32_t i = 0; i < nAlign; i++) any |= status[i] != 0;
+    if (!any) break;
+    if (pass == 1) rc = fail(ctx, OIC_ERR_OVERFLOW, "an alignment exceeds the engine's DP capacity");
+  }
+  if (rc == OIC_OK) {
+    CK(cudaMemcpy(out, dOut.p, (size_t)nAlign * 5 * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(kind, dKind.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(deltaLen, dDl.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
+    unsigned long long s2[2];
+    CK(cudaMemcpy(s2, ctr64(ctx) + kExtStatBase, sizeof(s2), cudaMemcpyDeviceToHost));
+    ctx->stats.dpCells += s2[0];
+    ctx->stats.slideBases += s2[1];
+  }
+  dP.release();
+  dOut.release();
+  dKind.release();
+  dDl.release();
+  dStatus.release();
+  return rc;
+}
+
+}  // extern "C"

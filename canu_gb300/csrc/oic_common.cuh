@@ -1,0 +1,199 @@
+// oic_common.cuh -- shared device-side definitions of the GB300 overlapInCore engine.
+//
+// Read layout in HBM: every read is packed 2 bits per base (A=0 C=1 G=2 T=3, base i
+// of a read at bits 2*(i%32) of 64-bit word i/32, the same order overlapInCore builds
+// its k-mer keys in, Build_Hash_Index.C:347-350) in two strand arrays -- forward and
+// reverse complement -- plus a parallel mask array with 0b11 at every N.  Reads start
+// on a word boundary and are separated by one zero guard word, so a 32-base window
+// that runs off either end of a read stays inside the arrays.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace oic {
+
+typedef unsigned long long u64;
+typedef long long          i64;
+typedef unsigned int       u32;
+
+constexpr u32 kMaxReadLenBits = 21;                              // AS_MAX_READLEN_BITS
+constexpr u32 kMaxReadLen     = (1u << kMaxReadLenBits) - 1;     // AS_MAX_READLEN
+constexpr int kHopelessMatch  = 90;                              // overlapInCore.H:78
+constexpr int kMaxDistinct    = 3;                               // overlapInCore.H:107
+constexpr int kMinIntersect   = 10;                              // overlapInCore.H:120
+constexpr int kShiftSlack     = 1;                               // overlapInCore.H:146
+constexpr int kEntriesPerBucket = 21;                            // overlapInCore.H:58
+constexpr u64 kEmptyKey       = ~0ull;
+constexpr u64 kPairMask       = 0x5555555555555555ull;
+
+// Device error flags (bitwise OR into ctx->dErr).  Kernels never trap: they record
+// the condition, skip the access and return.
+enum : u32 {
+  kErrBadBase      = 1u << 0,
+  kErrArenaFull    = 1u << 1,   // DP traceback arena of a warp exhausted
+  kErrBandWide     = 1u << 2,   // DP band wider than the shared-memory row buffer
+  kErrRowsFull     = 1u << 3,   // more DP rows than the row-header capacity
+  kErrNodePool     = 1u << 4,   // seed replay: node pool of a warp exhausted
+  kErrPairTable    = 1u << 5,   // seed replay: pair table of a warp exhausted
+  kErrOutNodes     = 1u << 6,   // global node output full
+  kErrOutPairs     = 1u << 7,   // global pair output full
+  kErrDeltaFull    = 1u << 8,
+  kErrTableFull    = 1u << 9,   // k-mer table probe ran through every slot
+  kErrInternal     = 1u << 10,
+  kErrNodesPerPair = 1u << 11
+};
+
+// Packed reads (device pointers).
+struct ReadsDev {
+  const u64 *fwd;       // forward strand words
+  const u64 *rc;        // reverse-complement strand words
+  const u64 *nfwd;      // N masks (0b11 per N) for the forward strand
+  const u64 *nrc;
+  const u64 *wordOff;   // first word of read i (0-based index = ID-1)
+  const u32 *len;
+  const u32 *lib;
+  const unsigned char *hasN;
+  u32 nReads;
+};
+
+// One read strand viewed as a base sequence: base i is at global base index gbase+i.
+struct SeqView {
+  const u64 *w;
+  const u64 *nm;   // nullptr when the read has no N
+  i64        gbase;
+};
+
+__device__ __forceinline__ SeqView make_view(const ReadsDev &R, u32 readIdx, int rev) {
+  SeqView v;
+  v.w     = rev ? R.rc : R.fwd;
+  v.nm    = R.hasN[readIdx] ? (rev ? R.nrc : R.nfwd) : nullptr;
+  v.gbase = (i64)R.wordOff[readIdx] * 32;
+  return v;
+}
+
+// 32 bases starting at global base index g (base g in bits 0-1).
+__device__ __forceinline__ u64 load_win(const u64 *w, i64 g) {
+  i64 wi = g >> 5;
+  int sh = (int)(g & 31) * 2;
+  u64 lo = __ldg(w + wi);
+  if (sh == 0) return lo;
+  u64 hi = __ldg(w + wi + 1);
+  return (lo >> sh) | (hi << (64 - sh));
+}
+
+// 32 bases g, g-1, ..., g-31 (base g in bits 0-1; the two bits of each base come out
+// swapped, which equality tests do not see).
+__device__ __forceinline__ u64 load_win_rev(const u64 *w, i64 g) { return __brevll(load_win(w, g - 31)); }
+
+// Number of leading bases (0..32) that agree between A (from a) and T (from t), with
+// N matching anything (prefixEditDistance-forward.C:164 / -reverse.C:186).
+template <int STEP>
+__device__ __forceinline__ int match_run32(const SeqView &A, i64 a, const SeqView &T, i64 t) {
+  u64 wa, wt;
+  if (STEP > 0) {
+    wa = load_win(A.w, A.gbase + a);
+    wt = load_win(T.w, T.gbase + t);
+  } else {
+    wa = load_win_rev(A.w, A.gbase + a);
+    wt = load_win_rev(T.w, T.gbase + t);
+  }
+  u64 x  = wa ^ wt;
+  u64 mm = (x | (x >> 1)) & kPairMask;
+  if (mm && (A.nm || T.nm)) {
+    u64 n = 0;
+    if (A.nm) n |= (STEP > 0) ? load_win(A.nm, A.gbase + a) : load_win_rev(A.nm, A.gbase + a);
+    if (T.nm) n |= (STEP > 0) ? load_win(T.nm, T.gbase + t) : load_win_rev(T.nm, T.gbase + t);
+    mm &= ~n;
+  }
+  return mm ? (__ffsll((long long)mm) - 1) >> 1 : 32;
+}
+
+// Bases that agree from A[step*row] / T[step*(row+d)] on, capped at `lim`.
+template <int STEP>
+__device__ __forceinline__ int slide(const SeqView &A, i64 a0, const SeqView &T, i64 t0, int row, int d, int lim,
+                                     unsigned long long &slides) {
+  int run = 0;
+  while (run < lim) {
+    int r = match_run32<STEP>(A, a0 + STEP * (i64)(row + run), T, t0 + STEP * (i64)(row + d + run));
+    run += r;
+    if (r < 32) break;
+  }
+  if (run > lim) run = lim;
+  slides += (unsigned long long)run;
+  return run;
+}
+
+__device__ __forceinline__ u64 mix64(u64 x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+
+// K-mer table (device).  vals: bits 0-31 first occurrence, 32-62 count, 63 screened.
+struct TableDev {
+  const u64 *keys;
+  const u64 *vals;
+  u64        mask;       // capacity - 1
+  const u64 *occ;        // (blockString << 32) | offset, ascending within a k-mer
+  const unsigned char *lscr, *rscr;   // String_Info l/rfrag_end_screened per block string
+  const u32 *slen;       // per block string: length (0 when the string is empty)
+  const u32 *sread;      // per block string: 0-based read index
+  u32        firstID;    // Hash_String_Num_Offset
+  u32        nStrings;
+};
+
+__device__ __forceinline__ bool table_find(const TableDev &T, u64 key, u64 &val) {
+  u64 s = mix64(key) & T.mask;
+  for (u64 probe = 0; probe <= T.mask; probe++) {
+    u64 k = __ldg(T.keys + s);
+    if (k == key) {
+      val = __ldg(T.vals + s);
+      return true;
+    }
+    if (k == kEmptyKey) return false;
+    s = (s + 1) & T.mask;
+  }
+  return false;
+}
+
+// Parameters every kernel needs (passed by value).
+struct DevParams {
+  double maxErate;
+  double branchMatchValue;     // prefixEditDistance.C:86
+  double minBranchTailSlope;   // prefixEditDistance.C:29
+  double kmerExpect;           // exp(-K * maxErate), host glibc
+  unsigned long long minKmers; // Filter_By_Kmer_Count after overlapInCore.C:410-411 (0 = off)
+  int    kmerLen;
+  int    partial;
+  int    unique;
+  int    hopeless;
+  int    minOlapLen;
+  int    maxErrors;            // MAX_ERRORS (prefixEditDistance.C:27)
+};
+
+__device__ __forceinline__ int error_bound(int i, double maxErate) {
+  return (int)ceil(__dmul_rn((double)i, maxErate));   // prefixEditDistance.C:60
+}
+
+// Warp helpers.
+__device__ __forceinline__ int warp_min(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_sum64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace oic

@@ -1,0 +1,117 @@
+// oic_kernels.cuh -- kernel launch wrappers shared between the .cu files and the
+// C-ABI layer.  Everything here runs on the context's stream.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "oic_common.cuh"
+#include "oic_align.cuh"
+
+namespace oic {
+
+// ---------------- reads ----------------
+// Pack ASCII reads into the 2-bit strand arrays (see oic_common.cuh).  err gets
+// kErrBadBase for a character outside ACGTN (either case).
+void launch_pack_reads(const char *ascii, const u64 *srcOff, const u32 *len, const u64 *wordOff, u32 nReads,
+                       u64 *fwd, u64 *rc, u64 *nfwd, u64 *nrc, unsigned char *hasN, u32 *err, cudaStream_t st);
+
+// ---------------- hash block ----------------
+// K-mer keys of every block string; key = 1 << 2K for a window holding an N.
+void launch_kmer_emit(ReadsDev R, const u32 *strRead, const u32 *strKmers, const u64 *flatStart, u32 nStr, int K,
+                      u64 *keys, u32 *vals, cudaStream_t st);
+// newKeys[s] += number of distinct k-mers whose first occurrence is in block string s.
+void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, int K, u32 *newKeys,
+                      cudaStream_t st);
+// flags[p] = 1 when keys[p] is a valid k-mer and vals[p] < flatLimit.
+void launch_keep_flags(const u64 *keys, const u32 *vals, u64 n, int K, u32 flatLimit, u32 *flags, cudaStream_t st);
+void launch_compact_kv(const u64 *keys, const u32 *vals, const u32 *flags, const u32 *pos, u64 n, u64 *keysOut,
+                       u32 *valsOut, cudaStream_t st);
+void launch_table_build(const u64 *keys, u64 n, u64 *tKeys, u64 *tVals, u64 mask, u32 *err, cudaStream_t st);
+void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, u64 *occ, cudaStream_t st);
+void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeysMut, u64 *tValsMut,
+                      unsigned char *lscr, unsigned char *rscr, int K, int hopeless, u32 *err, cudaStream_t st);
+
+// ---------------- seeds ----------------
+struct PairRec {
+  u32 sRead;      // 0-based read index of S
+  u32 tStr;       // block string index of T
+  u32 nodeOff;    // first match node in the node output
+  u32 nodeCnt;
+  int diagCt, diagBgn, diagEnd;
+  u32 flags;      // bit0 reverse strand, bit1 consistent, bit2 S left-end screened, bit3 S right-end screened
+};
+
+struct PairAcc {   // seed-replay state of one pair (per-warp scratch)
+  u32 T;
+  int head;
+  int diagCt, diagBgn, diagEnd;
+  int consistent;
+  int slot;
+  int pad;
+};
+
+struct SeedScratch {
+  int     *slotKey;    // per warp: slotCap ints
+  int     *slotVal;
+  PairAcc *pairs;      // per warp: pairCap
+  int4    *nodes;      // per warp: nodeCap (offset, len, start, next)
+};
+
+struct SeedCaps {
+  int slotCap;   // power of two
+  int pairCap;
+  int nodeCap;
+};
+
+struct SeedOut {
+  PairRec *pairs;
+  u32      pairCap;
+  u32     *pairCount;
+  int4    *nodes;       // (offset, len, start, unused)
+  u32      nodeCap;
+  u32     *nodeCount;
+  u32     *overflowSegs;
+  u32     *overflowCount;
+  unsigned long long *stats;   // [seeds, segments]
+  u32     *err;
+};
+
+void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, u32 nSeg, u32 *segCounter, SeedScratch sc,
+                 SeedCaps cap, int nWarps, SeedOut out, cudaStream_t st);
+
+// ---------------- pairs / DP ----------------
+struct AlignOut {
+  u32 *rec;             // 3 records x 6 words per pair slot
+  u32 *cnt;             // records per pair slot
+  u32 *overflow;        // pair indices that exceeded a capacity
+  u32 *overflowCount;
+  unsigned long long *stats;   // see StatIdx
+  u32 *err;
+};
+
+enum StatIdx {
+  kStWithoutOlap = 0, kStWithOlap, kStSkipped, kStMulti, kStTotal, kStContained, kStDovetail,
+  kStCells, kStSlides, kStExtensions, kStCount
+};
+
+// bandW selects the shared-memory configuration (compiled instances: 1024, 8192).
+void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs,
+                  const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap,
+                  int nWarps, AlignOut out, cudaStream_t st);
+
+struct ExtendProblem {
+  u32 sRead, sRev, tRead;
+  int mStart, mOffset, mLen;
+};
+void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
+                         WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
+                         unsigned long long *stats, cudaStream_t st);
+
+// Compact per-pair record slots into a dense record array.
+void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st);
+
+int align_warps_per_block(int bandW);
+size_t align_smem_bytes(int bandW);
+
+}  // namespace oic

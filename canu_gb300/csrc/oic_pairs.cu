@@ -1,0 +1,571 @@
+// oic_pairs.cu -- per-read-pair processing: Process_Matches with the warp DP.
+//
+// Reference: Process_Matches (overlapInCore-Process_String_Overlaps.C:354-547) takes a
+// pair's match list, repeatedly extends its longest remaining exact match with
+// Extend_Alignment, keeps dovetail results in at most three distinct overlaps
+// (Add_Overlap :175-244), drops the matches that lie on each alignment
+// (Lies_On_Alignment :260-281), then keeps one overlap per pair (Combine_Into_One_Olap
+// :40-96, or Merge_Intersecting_Olaps :106-162 with -m, Choose_Best_Partial :289-311
+// with -partial) and encodes it (Output_Overlap / Output_Partial_Overlap,
+// overlapInCore-Output.C:26-264).
+//
+// Here a persistent warp takes pairs from a queue; the node list is the array the seed
+// kernel wrote in list order, with an alive flag per node.  Pairs that exceed a
+// capacity of this configuration are queued for a wider configuration and leave no
+// output or counts behind.
+#include "oic_kernels.cuh"
+
+namespace oic {
+
+namespace {
+
+constexpr int kAlignWarpsSmall = 8;   // bandW 1024
+constexpr int kAlignWarpsLarge = 1;   // bandW 8192
+
+struct Olap {
+  int    s_lo, s_hi, t_lo, t_hi;
+  double quality;
+  int    delta_ct;
+  int    slb, srb, tlb, trb;     // s/t left/right boundaries
+  int    min_diag, max_diag;
+};
+
+// Add_Overlap (Process_String_Overlaps.C:175-244); every lane runs it identically.
+__device__ __forceinline__ void add_overlap(int partial, int s_lo, int s_hi, int t_lo, int t_hi, double q, int deltaCt,
+                                            Olap *o, int &ct) {
+  if (!partial) {
+    const int nd = t_lo - s_lo;
+    for (int i = 0; i < ct; i++) {
+      const int od = o[i].t_lo - o[i].s_lo;
+      if ((nd > 0 && od > 0 && o[i].trb - nd - o[i].slb >= kMinIntersect) ||
+          (nd <= 0 && od <= 0 && o[i].srb + nd - o[i].tlb >= kMinIntersect)) {
+        if (nd < o[i].min_diag) o[i].min_diag = nd;
+        if (nd > o[i].max_diag) o[i].max_diag = nd;
+        if (s_lo < o[i].slb) o[i].slb = s_lo;
+        if (s_hi > o[i].srb) o[i].srb = s_hi;
+        if (t_lo < o[i].tlb) o[i].tlb = t_lo;
+        if (t_hi > o[i].trb) o[i].trb = t_hi;
+        if (q < o[i].quality) {
+          o[i].s_lo = s_lo;
+          o[i].s_hi = s_hi;
+          o[i].t_lo = t_lo;
+          o[i].t_hi = t_hi;
+          o[i].quality  = q;
+          o[i].delta_ct = deltaCt;
+        }
+        return;
+      }
+    }
+  }
+  if (ct >= kMaxDistinct) return;
+  Olap &n = o[ct];
+  n.s_lo = n.slb = s_lo;
+  n.s_hi = n.srb = s_hi;
+  n.t_lo = n.tlb = t_lo;
+  n.t_hi = n.trb = t_hi;
+  n.quality  = q;
+  n.delta_ct = deltaCt;
+  n.min_diag = n.max_diag = t_lo - s_lo;
+  ct++;
+}
+
+__device__ __forceinline__ bool lies_on_alignment(const int *delta, int deltaLen, int start, int offset, int s_lo,
+                                                  int t_lo) {
+  int diag = t_lo - s_lo;
+  const int nd = offset - start;
+  for (int i = 0; i < deltaLen; i++) {
+    const int dl = delta[i];
+    s_lo += abs(dl);
+    if (start < s_lo) return abs(nd - diag) <= kShiftSlack;
+    if (dl < 0) diag++;
+    else {
+      s_lo++;
+      diag--;
+    }
+  }
+  return abs(nd - diag) <= kShiftSlack;
+}
+
+__device__ __forceinline__ void combine_into_one(Olap *o, int ct, int *deleted) {
+  int best = 0;
+  int mnd = o[0].min_diag, mxd = o[0].max_diag, slb = o[0].slb, srb = o[0].srb, tlb = o[0].tlb, trb = o[0].trb;
+  for (int i = 1; i < ct; i++) {
+    const int li = 1 + min(o[i].s_hi - o[i].s_lo, o[i].t_hi - o[i].t_lo);
+    const int lb = 1 + min(o[best].s_hi - o[best].s_lo, o[best].t_hi - o[best].t_lo);
+    if (o[i].quality < o[best].quality || (o[i].quality == o[best].quality && li > lb)) best = i;
+    mnd = min(mnd, o[i].min_diag);
+    mxd = max(mxd, o[i].max_diag);
+    slb = min(slb, o[i].slb);
+    srb = max(srb, o[i].srb);
+    tlb = min(tlb, o[i].tlb);
+    trb = max(trb, o[i].trb);
+  }
+  o[best].min_diag = mnd;
+  o[best].max_diag = mxd;
+  o[best].slb = slb;
+  o[best].srb = srb;
+  o[best].tlb = tlb;
+  o[best].trb = trb;
+  for (int i = 0; i < ct; i++) deleted[i] = (i != best);
+}
+
+__device__ __forceinline__ void merge_intersecting(Olap *p, int ct, int *deleted) {
+  for (int i = 0; i < ct - 1; i++)
+    for (int j = i + 1; j < ct; j++) {
+      if (deleted[i] || deleted[j]) continue;
+      const int lo = p[i].min_diag, hi = p[i].max_diag;
+      if ((lo <= 0 && p[j].min_diag > 0) || (lo > 0 && p[j].min_diag <= 0)) continue;
+      if ((lo >= 0 && p[j].trb - lo - p[j].slb >= kMinIntersect) ||
+          (lo <= 0 && p[j].srb + lo - p[j].tlb >= kMinIntersect) ||
+          (hi >= 0 && p[j].trb - hi - p[j].slb >= kMinIntersect) ||
+          (hi <= 0 && p[j].srb + hi - p[j].tlb >= kMinIntersect)) {
+        Olap *keep, *disc;
+        if (p[i].quality < p[j].quality) { keep = p + i; disc = p + j; deleted[j] = 1; }
+        else { keep = p + j; disc = p + i; deleted[i] = 1; }
+        keep->min_diag = min(keep->min_diag, disc->min_diag);
+        keep->max_diag = max(keep->max_diag, disc->max_diag);
+        keep->slb = min(keep->slb, disc->slb);
+        keep->srb = max(keep->srb, disc->srb);
+        keep->tlb = min(keep->tlb, disc->tlb);
+        keep->trb = max(keep->trb, disc->trb);
+      }
+    }
+}
+
+__device__ __forceinline__ void choose_best_partial(const Olap *o, int ct, int *deleted) {
+  int best = 0;
+  const double mb0 =
+      __dmul_rn(__dsub_rn(1.0, o[0].quality), (double)(2 + o[0].s_hi - o[0].s_lo + o[0].t_hi - o[0].t_lo));
+  for (int i = 1; i < ct; i++) {
+    const double mb =
+        __dmul_rn(__dsub_rn(1.0, o[i].quality), (double)(2 + o[i].s_hi - o[i].s_lo + o[i].t_hi - o[i].t_lo));
+    if (mb0 < mb || (mb0 == mb && o[i].quality < o[best].quality)) best = i;
+  }
+  for (int i = 0; i < ct; i++) deleted[i] = (i != best);
+}
+
+// AS_OVS_encodeEvalue (ovOverlap.H:35).
+__device__ __forceinline__ u32 encode_evalue(double q) {
+  return (q < 65535 / 100000.0) ? (u32)__dadd_rn(__dmul_rn(100000.0, q), 0.5) : 65535u;
+}
+
+// The span is accumulated in a 21-bit field one term at a time (Output.C:41-45).
+__device__ __forceinline__ u32 span21(const Olap &o) {
+  const u32 M21 = (1u << 21) - 1;
+  u32 sp = (u32)(o.s_hi - o.s_lo) & M21;
+  sp     = (sp + (u32)(o.t_hi - o.t_lo)) & M21;
+  sp     = (sp + (u32)o.delta_ct) & M21;
+  return sp / 2;
+}
+
+__device__ __forceinline__ void put_record(u32 *dst, u32 a, u32 b, u32 ahg5, u32 ahg3, u32 bhg5, u32 bhg3, u32 span,
+                                           u32 evalue, u32 flipped, u32 forOBT, u32 forDUP, u32 forUTG) {
+  const u64 M21 = (1u << 21) - 1;
+  const u64 d0 = ((u64)ahg5 & M21) | (((u64)ahg3 & M21) << 21) | (((u64)evalue & 0xffff) << 42) |
+                 ((u64)(flipped & 1) << 58) | ((u64)(forOBT & 1) << 59) | ((u64)(forDUP & 1) << 60) |
+                 ((u64)(forUTG & 1) << 61);
+  const u64 d1 = ((u64)bhg5 & M21) | (((u64)bhg3 & M21) << 21) | (((u64)span & M21) << 42);
+  dst[0] = a;
+  dst[1] = b;
+  dst[2] = (u32)(d0 >> 32);
+  dst[3] = (u32)d0;
+  dst[4] = (u32)(d1 >> 32);
+  dst[5] = (u32)d1;
+}
+
+struct PairCounts {
+  unsigned long long v[kStCount];
+};
+
+// Output_Overlap (Output.C:26-191).
+__device__ void output_overlap(u32 *dst, u32 sID, int sLen, int rev, u32 tID, int tLen, const Olap &o,
+                               PairCounts &pc) {
+  const int  sRH = sLen - o.s_hi - 1, tRH = tLen - o.t_hi - 1;
+  const bool sLeft = (o.s_lo > o.t_lo) || (o.s_lo == o.t_lo && sRH > tRH);
+  const u32  a = sLeft ? sID : tID, b = sLeft ? tID : sID;
+  char orient;
+  int  ahg, bhg;
+  if (sLeft) {
+    orient = rev ? 'O' : 'N';
+    ahg    = o.s_lo;
+    bhg    = tRH - sRH;
+  } else {
+    orient = rev ? 'I' : 'N';
+    ahg    = o.t_lo;
+    bhg    = sRH - tRH;
+  }
+  if (orient == 'O' && sRH >= tRH) {
+    orient = 'I';
+    ahg    = -(tRH - sRH);
+    bhg    = -(o.s_lo);
+  }
+  int ah, bh;
+  u32 flipped;
+  if (orient == 'O') { ah = -bhg; bh = -ahg; flipped = 1; }
+  else { ah = ahg; bh = bhg; flipped = (orient == 'I'); }
+  const u32 ahg5 = ah < 0 ? 0 : (u32)ah, bhg5 = ah < 0 ? (u32)(-ah) : 0;
+  const u32 bhg3 = bh < 0 ? 0 : (u32)bh, ahg3 = bh < 0 ? (u32)(-bh) : 0;
+  put_record(dst, a, b, ahg5, ahg3, bhg5, bhg3, span21(o), encode_evalue(o.quality), flipped, 0, 0, 1);
+  pc.v[kStTotal]++;
+  if (bhg <= 0) pc.v[kStContained]++;
+  else pc.v[kStDovetail]++;
+}
+
+// Output_Partial_Overlap (Output.C:195-264).
+__device__ void output_partial(u32 *dst, u32 sID, u32 tID, int rev, const Olap &o, int sLen, int tLen,
+                               PairCounts &pc) {
+  u32 ahg5, ahg3, bhg5, bhg3;
+  if (!rev) {
+    ahg5 = (u32)o.s_lo;
+    ahg3 = (u32)(sLen - (o.s_hi + 1));
+    bhg5 = (u32)o.t_lo;
+    bhg3 = (u32)(tLen - (o.t_hi + 1));
+  } else {
+    ahg5 = (u32)(sLen - (o.s_hi + 1));
+    ahg3 = (u32)o.s_lo;
+    bhg5 = (u32)(tLen - (o.t_hi + 1));
+    bhg3 = (u32)o.t_lo;
+  }
+  put_record(dst, sID, tID, ahg5, ahg3, bhg5, bhg3, span21(o), encode_evalue(o.quality), rev ? 1u : 0u, 1, 1, 0);
+  pc.v[kStTotal]++;
+}
+
+__device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &base, const AlignCaps &cap, u64 gw) {
+  WarpScratch s;
+  s.arena  = base.arena + gw * (u64)cap.arenaCap;
+  s.rowOff = base.rowOff + gw * (u64)cap.rowCap;
+  s.rowL   = base.rowL + gw * (u64)cap.rowCap;
+  s.rowR   = base.rowR + gw * (u64)cap.rowCap;
+  s.deltaL = base.deltaL + gw * (u64)(cap.rowCap + 8);
+  s.deltaR = base.deltaR + gw * (u64)(cap.rowCap + 8);
+  s.stack  = base.stack + gw * (u64)(cap.rowCap + 8);
+  s.alive  = base.alive + gw * (u64)cap.nodeCap;
+  return s;
+}
+
+// Process_Matches for one pair.  Returns false on a capacity overflow (nothing was
+// written, pc untouched).
+__device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, const PairRec &pr, const int4 *nodesAll,
+                             u32 *recOut, u32 &nRec, PairCounts &pcOut) {
+  const int lane = threadIdx.x & 31;
+  const DevParams &P = w.P;
+  PairCounts pc;
+#pragma unroll
+  for (int i = 0; i < kStCount; i++) pc.v[i] = 0;
+  nRec = 0;
+
+  const u32 sRead = pr.sRead;
+  const int rev   = pr.flags & 1;
+  const int cons  = (pr.flags >> 1) & 1;
+  const bool segL = (pr.flags >> 2) & 1, segR = (pr.flags >> 3) & 1;
+  const SeqView S = make_view(R, sRead, rev);
+  const int sLen  = (int)R.len[sRead];
+  const u32 sID   = sRead + 1;
+  const u32 tRead = Tb.sread[pr.tStr];
+  const SeqView T = make_view(R, tRead, 0);
+  const int tLen  = (int)R.len[tRead];
+  const u32 tID   = tRead + 1;
+  const bool tLs = Tb.lscr[pr.tStr] != 0, tRs = Tb.rscr[pr.tStr] != 0;
+
+  // --minkmers (computeMinimumKmers, Process_String_Overlaps.C:21-33, :618-621)
+  if (P.minKmers) {
+    double ol = (double)(pr.diagEnd - pr.diagBgn);
+    if (ol < 0) ol = -ol;
+    unsigned long long ex = 0;
+    if (!(ol < (double)P.kmerLen))
+      ex = (unsigned long long)(long long)(int)floor(__dmul_rn(P.kmerExpect, __dadd_rn(__dsub_rn(ol, (double)P.kmerLen), 1.0)));
+    const unsigned long long need = P.minKmers > ex ? P.minKmers : ex;
+    if (need > (unsigned long long)(long long)pr.diagCt) {
+      pc.v[kStSkipped]++;
+      pcOut = pc;
+      return true;
+    }
+  }
+
+  const int4 *nodes = nodesAll + pr.nodeOff;
+  const int   cnt   = (int)pr.nodeCnt;
+  if (cnt <= 0) {
+    pc.v[kStWithoutOlap]++;
+    pcOut = pc;
+    return true;
+  }
+
+  // Hopeless check for a single match (:384-415).
+  if (P.hopeless && cnt == 1 && !P.partial) {
+    const int4 m = nodes[0];   // x offset, y len, z start
+    bool hopeless = false;
+    const int sHead = m.z, tHead = m.x;
+    if (sHead <= tHead) {
+      if (sHead > kHopelessMatch && !segL) hopeless = true;
+    } else {
+      if (tHead > kHopelessMatch && !tLs) hopeless = true;
+    }
+    const int sTail = sLen - sHead - m.y + 1, tTail = tLen - tHead - m.y + 1;
+    if (sTail <= tTail) {
+      if (sTail > kHopelessMatch && !segR) hopeless = true;
+    } else {
+      if (tTail > kHopelessMatch && !tRs) hopeless = true;
+    }
+    if (hopeless) {
+      pc.v[kStWithoutOlap]++;
+      pcOut = pc;
+      return true;
+    }
+  }
+
+  if (cnt > w.cap.nodeCap) {
+    w.err |= kErrNodesPerPair;
+    return false;
+  }
+  for (int i = lane; i < cnt; i += 32) w.sc.alive[i] = 1;
+  __syncwarp();
+
+  Olap olap[kMaxDistinct];
+  int  nOlap = 0;
+  const unsigned long long cells0 = w.cells, slides0 = w.slides;
+
+  while (true) {
+    // Longest remaining match, first in list order on ties (:424-431).
+    int myLen = -1, myIdx = INT_MAX;
+    for (int i = lane; i < cnt; i += 32)
+      if (w.sc.alive[i] && nodes[i].y > myLen) {
+        myLen = nodes[i].y;
+        myIdx = i;
+      }
+    const int maxLen = warp_max(myLen);
+    if (maxLen < 0) break;
+    const int li = warp_min(myLen == maxLen ? myIdx : INT_MAX);
+    const int4 lm = nodes[li];
+
+    int sLo = 0, sHi = 0, tLo = 0, tHi = 0, errors = 0;
+    const int kind = warp_extend(w, S, sLen, T, tLen, lm.z, lm.x, lm.y, sLo, sHi, tLo, tHi, errors);
+    if (w.err) {
+      w.cells  = cells0;
+      w.slides = slides0;
+      return false;
+    }
+    pc.v[kStExtensions]++;
+
+    const bool dov = (kind == kDovetail) || P.partial;
+    if (dov && 1 + sHi - sLo >= P.minOlapLen && 1 + tHi - tLo >= P.minOlapLen) {
+      const int    olapLen = 1 + min(sHi - sLo, tHi - tLo);
+      const double quality = __ddiv_rn((double)errors, (double)olapLen);
+      if (errors <= error_bound(olapLen, P.maxErate))
+        add_overlap(P.partial, sLo, sHi, tLo, tHi, quality, w.leftLen, olap, nOlap);
+    }
+    if (cons) break;
+
+    // Drop the longest match and every match that lies on the alignment (:476-490).
+    for (int i = lane; i < cnt; i += 32) {
+      if (!w.sc.alive[i]) continue;
+      const int4 q = nodes[i];
+      bool rm = (i == li);
+      if (!rm && dov && sLo - kShiftSlack <= q.z && q.z + q.y <= (sHi + 1) + kShiftSlack - 1 &&
+          lies_on_alignment(w.sc.deltaL, w.leftLen, q.z, q.x, sLo, tLo))
+        rm = true;
+      if (rm) w.sc.alive[i] = 0;
+    }
+    __syncwarp();
+  }
+
+  int nOut = 0;
+  if (nOlap > 0) {
+    int deleted[kMaxDistinct] = {0, 0, 0};
+    if (P.partial) {
+      if (P.unique) choose_best_partial(olap, nOlap, deleted);
+    } else {
+      if (P.unique) combine_into_one(olap, nOlap, deleted);
+      else merge_intersecting(olap, nOlap, deleted);
+    }
+    for (int i = 0; i < nOlap; i++)
+      if (!deleted[i]) {
+        u32 rec[6];
+        if (P.partial) output_partial(rec, sID, tID, rev, olap[i], sLen, tLen, pc);
+        else output_overlap(rec, sID, sLen, rev, tID, tLen, olap[i], pc);
+        if (lane == 0)
+          for (int k = 0; k < 6; k++) recOut[nOut * 6 + k] = rec[k];
+        nOut++;
+      }
+  }
+  if (nOut == 0) pc.v[kStWithoutOlap]++;
+  else {
+    pc.v[kStWithOlap]++;
+    if (nOut > 1) pc.v[kStMulti]++;
+  }
+  nRec  = (u32)nOut;
+  pcOut = pc;
+  return true;
+}
+
+template <int BANDW, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
+                                                           const PairRec *pairs, const u32 *work, u32 nWork,
+                                                           u32 *workCounter, const int4 *nodes, WarpScratch scBase,
+                                                           AlignCaps cap, AlignOut out) {
+  extern __shared__ int smemRows[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const u64 gw   = (u64)blockIdx.x * WARPS + wib;
+
+  WarpDP w;
+  w.sc     = warp_scratch(scBase, cap, gw);
+  w.cap    = cap;
+  w.smA    = smemRows + (size_t)wib * 2 * BANDW;
+  w.smB    = w.smA + BANDW;
+  w.eml    = eml;
+  w.P      = P;
+  w.cells  = 0;
+  w.slides = 0;
+  w.err    = 0;
+  w.leftLen = w.rightLen = 0;
+
+  PairCounts acc;
+#pragma unroll
+  for (int i = 0; i < kStCount; i++) acc.v[i] = 0;
+
+  while (true) {
+    u32 k = 0;
+    if (lane == 0) k = atomicAdd(workCounter, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= nWork) break;
+    const u32 pi = work[k];
+    const PairRec pr = pairs[pi];
+    u32 nRec = 0;
+    PairCounts pc;
+    w.err = 0;
+    const bool ok = process_pair(w, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, pc);
+    if (ok) {
+      if (lane == 0) out.cnt[pi] = nRec;
+#pragma unroll
+      for (int i = 0; i < kStCount; i++) acc.v[i] += pc.v[i];
+    } else {
+      if (lane == 0) {
+        out.cnt[pi] = 0;
+        u32 slot = atomicAdd(out.overflowCount, 1u);
+        out.overflow[slot] = pi;
+        atomicOr(out.err, w.err);
+      }
+    }
+    __syncwarp();
+  }
+  // Cells are warp-uniform; slides are counted per lane.
+  const unsigned long long slidesWarp = warp_sum64(w.slides);
+  if (lane == 0) {
+    acc.v[kStCells] += w.cells;
+    acc.v[kStSlides] += slidesWarp;
+#pragma unroll
+    for (int i = 0; i < kStCount; i++)
+      if (acc.v[i]) atomicAdd(&out.stats[i], acc.v[i]);
+  }
+}
+
+template <int BANDW, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) extend_batch_kernel(ReadsDev R, DevParams P, const int *eml,
+                                                                  const ExtendProblem *probs, u32 n, WarpScratch scBase,
+                                                                  AlignCaps cap, int *out, int *kind, int *deltaLen,
+                                                                  u32 *status, unsigned long long *stats) {
+  extern __shared__ int smemRows[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const u64 gw   = (u64)blockIdx.x * WARPS + wib;
+  const u64 nw   = (u64)gridDim.x * WARPS;
+
+  WarpDP w;
+  w.sc     = warp_scratch(scBase, cap, gw);
+  w.cap    = cap;
+  w.smA    = smemRows + (size_t)wib * 2 * BANDW;
+  w.smB    = w.smA + BANDW;
+  w.eml    = eml;
+  w.P      = P;
+  w.cells  = 0;
+  w.slides = 0;
+  w.err    = 0;
+  w.leftLen = w.rightLen = 0;
+
+  for (u64 i = gw; i < n; i += nw) {
+    const ExtendProblem pb = probs[i];
+    const SeqView S = make_view(R, pb.sRead, pb.sRev ? 1 : 0);
+    const SeqView T = make_view(R, pb.tRead, 0);
+    const int sLen = (int)R.len[pb.sRead], tLen = (int)R.len[pb.tRead];
+    int sLo = 0, sHi = 0, tLo = 0, tHi = 0, errors = 0;
+    w.err = 0;
+    const int k = warp_extend(w, S, sLen, T, tLen, pb.mStart, pb.mOffset, pb.mLen, sLo, sHi, tLo, tHi, errors);
+    if (lane == 0) {
+      out[5 * i + 0] = sLo;
+      out[5 * i + 1] = sHi;
+      out[5 * i + 2] = tLo;
+      out[5 * i + 3] = tHi;
+      out[5 * i + 4] = errors;
+      kind[i]        = k;
+      deltaLen[i]    = w.leftLen;
+      status[i]      = w.err;
+    }
+    __syncwarp();
+  }
+  const unsigned long long slidesWarp = warp_sum64(w.slides);
+  if (lane == 0) {
+    atomicAdd(&stats[0], w.cells);
+    atomicAdd(&stats[1], slidesWarp);
+  }
+}
+
+__global__ void compact_records_kernel(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst) {
+  for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p < nPairs; p += gridDim.x * blockDim.x) {
+    const u32 c = cnt[p];
+    for (u32 j = 0; j < c * 6; j++) dst[(u64)pos[p] * 6 + j] = rec[(u64)p * 18 + j];
+  }
+}
+
+}  // namespace
+
+int align_warps_per_block(int bandW) { return bandW <= 1024 ? kAlignWarpsSmall : kAlignWarpsLarge; }
+
+size_t align_smem_bytes(int bandW) {
+  const int b = bandW <= 1024 ? 1024 : 8192;
+  return (size_t)align_warps_per_block(bandW) * 2 * b * sizeof(int);
+}
+
+void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs, const u32 *work,
+                  u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap, int nWarps,
+                  AlignOut out, cudaStream_t st) {
+  if (nWork == 0) return;
+  const int wpb = align_warps_per_block(bandW);
+  const int blocks = (nWarps + wpb - 1) / wpb;
+  const size_t smem = align_smem_bytes(bandW);
+  cap.bandW = bandW <= 1024 ? 1024 : 8192;
+  if (bandW <= 1024) {
+    auto k = align_kernel<1024, kAlignWarpsSmall>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
+  } else {
+    auto k = align_kernel<8192, kAlignWarpsLarge>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
+  }
+}
+
+void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
+                         WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
+                         unsigned long long *stats, cudaStream_t st) {
+  if (n == 0) return;
+  const int wpb = align_warps_per_block(bandW);
+  const int blocks = (nWarps + wpb - 1) / wpb;
+  const size_t smem = align_smem_bytes(bandW);
+  cap.bandW = bandW <= 1024 ? 1024 : 8192;
+  if (bandW <= 1024) {
+    auto k = extend_batch_kernel<1024, kAlignWarpsSmall>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
+  } else {
+    auto k = extend_batch_kernel<8192, kAlignWarpsLarge>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
+  }
+}
+
+void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st) {
+  if (nPairs == 0) return;
+  unsigned g = (nPairs + 255) / 256;
+  if (g > 65535u * 8) g = 65535u * 8;
+  compact_records_kernel<<<g, 256, 0, st>>>(rec, cnt, pos, nPairs, dst);
+}
+
+}  // namespace oic

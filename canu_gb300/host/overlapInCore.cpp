@@ -1,0 +1,278 @@
+// overlapInCore -- drop-in command line for canu's overlap stage on one GB300.
+//
+// Takes the reference's command line (overlapInCore.C:283-450) and writes what it
+// writes: the overlap records of ovFile(ovFileFullWrite) (ovStoreFile.C:212-286) to -o,
+// the <prefix>.oc per-read counts (ovStoreFile.H:50-115) and the -s stats file
+// (overlapInCore.C:539-560).  All overlap computation happens in liboic_gpu.so.
+//
+// Differences from the reference command line:
+//   * the positional store argument is an oic_seqdb read container (include/oic_seqdb.h);
+//   * -l <n> (a per-read overlap cap that makes read pairs depend on each other) is
+//     rejected;
+//   * --gpu-device <d> picks the CUDA device, --ovb-snappy frames the records in snappy
+//     blocks as ovFile does (default: the six-word records unframed).
+#include <cerrno>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "oic_gpu.h"
+#include "oic_seqdb.h"
+
+namespace {
+
+bool isFile(const char *p) {
+  struct stat st;
+  return p && stat(p, &st) == 0 && S_ISREG(st.st_mode);
+}
+
+void decodeRange(const char *s, uint32_t &bgn, uint32_t &end) {
+  char *e = nullptr;
+  bgn     = (uint32_t)strtoul(s, &e, 10);
+  end     = bgn;
+  if (e && *e == '-') end = (uint32_t)strtoul(e + 1, nullptr, 10);
+}
+
+void usage(const char *prog) {
+  fprintf(stderr, "USAGE:  %s [options] <seqStorePath>\n", prog);
+  fprintf(stderr, "  -partial -h a-b -H a-b -r a-b -R a-b -k <int|file> -m -u -z -t <n>\n");
+  fprintf(stderr, "  --hashbits n --hashdatalen n --hashload f --maxerate f --alignnoise f\n");
+  fprintf(stderr, "  --minlength n --minkmers -o out.ovb -s out.stats [--gpu-device d] [--ovb-snappy]\n");
+}
+
+// Mark_Skip_Kmers file format (Build_Hash_Index.C:203-246): one k-mer per line (first
+// whitespace-delimited token), FASTA '>' header lines skipped.
+int readSkipFile(const char *path, uint32_t K, std::string &out) {
+  FILE *F = fopen(path, "r");
+  if (!F) {
+    fprintf(stderr, "Failed to open '%s': %s\n", path, strerror(errno));
+    return 1;
+  }
+  char line[1024];
+  int  lineNum = 0;
+  while (fgets(line, sizeof(line), F)) {
+    lineNum++;
+    if (line[0] == '>') {
+      if (!fgets(line, sizeof(line), F)) break;
+      lineNum++;
+    }
+    for (int i = 0; line[i]; i++)
+      if (line[i] == ' ' || line[i] == '\t' || line[i] == '\n' || line[i] == '\r') line[i] = 0;
+    size_t len = strlen(line);
+    if (len != K) {
+      fprintf(stderr, "Short kmer skip kmer '%s' at line %d, expecting length %u got length %zu.\n", line, lineNum, K,
+              len);
+      fclose(F);
+      return 1;
+    }
+    out.append(line, K);
+  }
+  fclose(F);
+  return 0;
+}
+
+// ---- snappy framing (literal-only blocks), the stream format ovFile::writeBuffer emits
+// ([u64 compressed length][snappy raw block] per buffer; ovStoreFile.C:212-248).  A
+// literal-only block is a valid snappy encoding: the uncompressed length as a varint,
+// then literal elements of at most 64 KiB.
+void putVarint(std::vector<uint8_t> &b, uint64_t v) {
+  while (v >= 0x80) {
+    b.push_back((uint8_t)(v | 0x80));
+    v >>= 7;
+  }
+  b.push_back((uint8_t)v);
+}
+
+void snappyLiteralBlock(const uint8_t *src, size_t n, std::vector<uint8_t> &dst) {
+  dst.clear();
+  putVarint(dst, n);
+  size_t p = 0;
+  while (p < n) {
+    size_t k = std::min<size_t>(n - p, 65536);
+    size_t l = k - 1;
+    if (l < 60) dst.push_back((uint8_t)(l << 2));
+    else if (l < 256) { dst.push_back(60 << 2); dst.push_back((uint8_t)l); }
+    else { dst.push_back(61 << 2); dst.push_back((uint8_t)(l & 0xff)); dst.push_back((uint8_t)(l >> 8)); }
+    dst.insert(dst.end(), src + p, src + p + k);
+    p += k;
+  }
+}
+
+int writeOvb(const char *path, const std::vector<uint32_t> &rec, bool snappy) {
+  FILE *F = fopen(path, "wb");
+  if (!F) {
+    fprintf(stderr, "Failed to open '%s' for writing: %s\n", path, strerror(errno));
+    return 1;
+  }
+  bool bad = false;
+  if (!snappy) {
+    if (!rec.empty()) bad = fwrite(rec.data(), 4, rec.size(), F) != rec.size();
+  } else {
+    // ovFile buffer: a whole number of 6-word records, lcm of the two record sizes
+    // (ovStoreFile.C:112-121), default 1 MiB buffer.
+    const size_t lcm = (4 * 1 + 16) * (4 * 2 + 16);
+    const size_t bufWords = ((1024 * 1024) / (lcm * 4)) * lcm;
+    std::vector<uint8_t> blk;
+    for (size_t p = 0; p < rec.size(); p += bufWords) {
+      size_t   n = std::min(bufWords, rec.size() - p);
+      snappyLiteralBlock((const uint8_t *)(rec.data() + p), n * 4, blk);
+      uint64_t bl = blk.size();
+      bad |= fwrite(&bl, 8, 1, F) != 1;
+      bad |= fwrite(blk.data(), 1, blk.size(), F) != blk.size();
+    }
+  }
+  bad |= fclose(F) != 0;
+  return bad ? 1 : 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  oic_params P;
+  oic_default_params(&P);
+  P.numThreads = 1;
+  const char *store = nullptr, *outName = nullptr, *statName = nullptr, *skipFile = nullptr;
+  int         device = 0, err = 0;
+  bool        snappy = false;
+
+  for (int a = 1; a < argc; a++) {
+    const char *o   = argv[a];
+    auto        nxt = [&]() -> const char * {
+      if (a + 1 >= argc) { err++; return "0"; }
+      return argv[++a];
+    };
+    if (!strcmp(o, "-partial")) P.partial = 1;
+    else if (!strcmp(o, "-h")) decodeRange(nxt(), P.bgnHashID, P.endHashID);
+    else if (!strcmp(o, "-H")) decodeRange(nxt(), P.minLibToHash, P.maxLibToHash);
+    else if (!strcmp(o, "-r")) decodeRange(nxt(), P.bgnRefID, P.endRefID);
+    else if (!strcmp(o, "-R")) decodeRange(nxt(), P.minLibToRef, P.maxLibToRef);
+    else if (!strcmp(o, "-k")) {
+      const char *v = nxt();
+      if (isFile(v)) skipFile = v;
+      else P.kmerLen = (uint32_t)strtoul(v, nullptr, 10);
+    } else if (!strcmp(o, "-l")) {
+      long l = strtol(nxt(), nullptr, 10);
+      if (l >= 1) {
+        fprintf(stderr, "-l (per-read overlap limit) is not supported by this overlapper\n");
+        err++;
+      }
+    } else if (!strcmp(o, "-m")) P.uniqueOlapPerPair = 0;
+    else if (!strcmp(o, "-u")) P.uniqueOlapPerPair = 1;
+    else if (!strcmp(o, "--hashbits")) P.hashBits = (uint32_t)strtoull(nxt(), nullptr, 10);
+    else if (!strcmp(o, "--hashdatalen")) P.maxHashDataLen = strtoull(nxt(), nullptr, 10);
+    else if (!strcmp(o, "--hashload")) P.maxHashLoad = atof(nxt());
+    else if (!strcmp(o, "-o")) outName = nxt();
+    else if (!strcmp(o, "-s")) statName = nxt();
+    else if (!strcmp(o, "-t")) {
+      long t = strtol(nxt(), nullptr, 10);
+      P.numThreads = (uint32_t)(t < 1 ? 1 : t);
+    } else if (!strcmp(o, "--minlength")) P.minOlapLen = (int32_t)strtol(nxt(), nullptr, 10);
+    else if (!strcmp(o, "--minkmers")) P.minKmers = 1;
+    else if (!strcmp(o, "--maxerate")) P.maxErate = strtof(nxt(), nullptr);     // overlapInCore.C:380
+    else if (!strcmp(o, "--alignnoise")) P.alignNoise = strtof(nxt(), nullptr);
+    else if (!strcmp(o, "-z")) P.useHopelessCheck = 0;
+    else if (!strcmp(o, "--gpu-device")) device = atoi(nxt());
+    else if (!strcmp(o, "--ovb-snappy")) snappy = true;
+    else if (!store) store = o;
+    else {
+      fprintf(stderr, "Unknown option '%s'\n", o);
+      err++;
+    }
+  }
+  if (P.kmerLen == 0) fprintf(stderr, "* No kmer length supplied; -k needed!\n"), err++;
+  if (!outName) fprintf(stderr, "ERROR:  No output file name specified\n"), err++;
+  if (err || !store) {
+    usage(argv[0]);
+    return 1;
+  }
+
+  oic_seqdb db;
+  if (oic_seqdb_load(store, &db)) {
+    fprintf(stderr, "Failed to load read container '%s'\n", store);
+    return 1;
+  }
+  oic_ctx *ctx = nullptr;
+  int      rc  = oic_create(&P, device, &ctx);
+  if (rc) {
+    fprintf(stderr, "oic_create failed (%d): %s\n", rc, ctx ? oic_last_error(ctx) : "bad parameters or no CUDA device");
+    return 1;
+  }
+  std::vector<uint32_t> lib(db.nReads), len(db.nReads);
+  std::vector<uint64_t> off(db.nReads);
+  for (uint32_t i = 0; i < db.nReads; i++) {
+    lib[i] = db.index[i].libID;
+    len[i] = db.index[i].length;
+    off[i] = db.index[i].offset;
+  }
+  rc = oic_set_reads(ctx, db.nReads, lib.data(), len.data(), off.data(), db.bases, db.nBases);
+  if (!rc && skipFile) {
+    std::string kmers;
+    if (readSkipFile(skipFile, P.kmerLen, kmers)) return 1;
+    rc = oic_set_skip_kmers(ctx, kmers.data(), kmers.size() / P.kmerLen);
+    fprintf(stderr, "\nRead %zu kmers to mark to skip\n\n", kmers.size() / P.kmerLen);
+  }
+  if (!rc) rc = oic_run(ctx);
+  if (rc) {
+    fprintf(stderr, "overlapInCore failed (%d): %s\n", rc, oic_last_error(ctx));
+    oic_destroy(ctx);
+    return 1;
+  }
+
+  uint64_t n = 0;
+  oic_num_overlaps(ctx, &n);
+  std::vector<uint32_t> rec((size_t)n * 6);
+  oic_fetch_overlaps(ctx, rec.data(), n, &n);
+  oic_stats st;
+  oic_get_stats(ctx, &st);
+  oic_destroy(ctx);
+
+  if (writeOvb(outName, rec, snappy)) return 1;
+
+  // <prefix>.oc: u64 nOlaps, u32 oprMax, u32 opr[oprMax] (ovStoreFile.H:73-91).
+  std::string oc = outName;
+  if (oc.size() > 4 && oc.compare(oc.size() - 4, 4, ".ovb") == 0) oc.resize(oc.size() - 4);
+  oc += ".oc";
+  uint32_t              oprMax = db.nReads + 1;
+  std::vector<uint32_t> opr(oprMax, 0);
+  for (uint64_t i = 0; i < n; i++) {
+    opr[rec[6 * i + 0]]++;
+    opr[rec[6 * i + 1]]++;
+  }
+  if (FILE *C = fopen(oc.c_str(), "wb")) {
+    fwrite(&n, 8, 1, C);
+    fwrite(&oprMax, 4, 1, C);
+    fwrite(opr.data(), 4, oprMax, C);
+    fclose(C);
+  }
+
+  FILE *S = stderr;
+  if (statName) {
+    S = fopen(statName, "w");
+    if (!S) {
+      fprintf(stderr, "WARNING: failed to open '%s' for writing: %s\n", statName, strerror(errno));
+      S = stderr;
+    }
+  }
+  fprintf(S, " Kmer hits without olaps = %ld\n", (long)st.kmerHitsWithoutOlap);
+  fprintf(S, "    Kmer hits with olaps = %ld\n", (long)st.kmerHitsWithOlap);
+  fprintf(S, "  Multiple overlaps/pair = %ld\n", (long)st.multiOverlap);
+  fprintf(S, " Total overlaps produced = %ld\n", (long)st.totalOverlaps);
+  fprintf(S, "      Contained overlaps = %ld\n", (long)st.containedOverlaps);
+  fprintf(S, "       Dovetail overlaps = %ld\n", (long)st.dovetailOverlaps);
+  fprintf(S, "Rejected by short window = %ld\n", (long)st.badShortWindow);
+  fprintf(S, " Rejected by long window = %ld\n", (long)st.badLongWindow);
+  if (S != stderr) fclose(S);
+
+  fprintf(stderr, "GPU: %lu overlaps; %lu seeds, %lu pairs, %lu extensions, %lu DP cells; hash %.2f ms, seed %.2f ms, "
+                  "align %.2f ms, total %.2f ms\n",
+          (unsigned long)n, (unsigned long)st.seeds, (unsigned long)st.candidatePairs, (unsigned long)st.extensions,
+          (unsigned long)st.dpCells, st.msHash, st.msSeed, st.msAlign, st.msTotal);
+  fprintf(stderr, "Bye.\n");
+  oic_seqdb_free(&db);
+  return 0;
+}

@@ -124,6 +124,8 @@ struct Options {
   uint32_t skipK       = 22;
   uint32_t skipMin     = 11;
   std::string genomeOut;
+  double   nRate       = 0.0;   // per-base chance that a read base is reported as N
+  uint32_t libs        = 1;     // library IDs drawn uniformly from 1..libs
 };
 
 void usage() {
@@ -133,7 +135,8 @@ void usage() {
           "  [--pareto-alpha A] [--err E] [--ratio sub:ins:del] [--rc-frac F]\n"
           "  [--repeat-copies N] [--repeat-len W] [--repeat-div D]\n"
           "  [--tandem-frac F] [--tandem-unit U] [--tandem-div D] [--seed S]\n"
-          "  [--skip-out kmers.txt --skip-k K --skip-min-count C] [--genome-out g.txt]\n");
+          "  [--skip-out kmers.txt --skip-k K --skip-min-count C] [--genome-out g.txt]\n"
+          "  [--n-rate P] [--libs L]\n");
   exit(1);
 }
 
@@ -169,6 +172,8 @@ Options parse(int argc, char **argv) {
     else if (a == "--skip-k") o.skipK = (uint32_t)strtoul(val(), NULL, 10);
     else if (a == "--skip-min-count") o.skipMin = (uint32_t)strtoul(val(), NULL, 10);
     else if (a == "--genome-out") o.genomeOut = val();
+    else if (a == "--n-rate") o.nRate = atof(val());
+    else if (a == "--libs") o.libs = (uint32_t)strtoul(val(), NULL, 10);
     else usage();
   }
   if (o.out.empty() && o.genomeOut.empty()) usage();
@@ -304,7 +309,7 @@ int main(int argc, char **argv) {
   double pSub = o.rSub / (o.rSub + o.rIns + o.rDel);
   double pIns = o.rIns / (o.rSub + o.rIns + o.rDel);
 
-  std::vector<uint32_t> lens;
+  std::vector<uint32_t> lens, libs;
   std::string           bases;
   double                target = o.coverage * (double)o.genome;
   double                total  = 0;
@@ -334,11 +339,14 @@ int main(int argc, char **argv) {
       for (auto &b : read) b = complement(b);
     }
     if (read.empty()) continue;
+    if (o.nRate > 0)
+      for (auto &b : read)
+        if (r.uniform() < o.nRate) b = 'N';
+    libs.push_back(o.libs > 1 ? 1 + (uint32_t)r.below(o.libs) : 1);
     lens.push_back((uint32_t)read.size());
     bases += read;
     total += (double)L;
   }
-  std::vector<uint32_t> libs(lens.size(), 1);
   if (oic_seqdb_write(o.out.c_str(), (uint32_t)lens.size(), libs.data(), lens.data(), bases.data()) != 0) {
     fprintf(stderr, "oic_synth: failed to write '%s'\n", o.out.c_str());
     return 1;

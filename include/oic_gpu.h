@@ -1,0 +1,139 @@
+/*
+ * oic_gpu.h -- C ABI of the GB300 overlapInCore engine (liboic_gpu.so).
+ *
+ * The library is the drop-in for canu's overlapInCore hot path: the k-mer hash
+ * block, the seed lookup and per-read-pair bucketing, and the banded prefix edit
+ * distance extension that turns seeds into ovOverlap records.  All compute runs in
+ * hand-written sm_103a CUDA kernels on one GPU; there is no CPU fallback: every
+ * entry point returns OIC_ERR_CUDA when the device or the kernels are unavailable.
+ *
+ * Plain C types only: pointers, sizes, status codes.  All host buffers are owned by
+ * the caller.  A context is single-threaded and owns one CUDA stream.
+ *
+ * Record format: one overlap = six uint32 words, exactly what canu's ovFile writes
+ * for an ovFileFullWrite record (src/stores/ovStoreFile.C:262-276):
+ *   a_iid, b_iid, dat[0] >> 32, dat[0] & 0xffffffff, dat[1] >> 32, dat[1] & 0xffffffff
+ * with the ovOverlapDAT bit layout of AS_MAX_READLEN_BITS == 21
+ * (src/stores/ovOverlap.H:55-78).
+ */
+#ifndef OIC_GPU_H
+#define OIC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  0 is success. */
+enum {
+  OIC_OK             = 0,
+  OIC_ERR_ARG        = 1,   /* bad argument / unsupported option                     */
+  OIC_ERR_INPUT      = 2,   /* input the reference rejects (bad base, short read ...) */
+  OIC_ERR_CUDA       = 3,   /* CUDA runtime error or no usable device                 */
+  OIC_ERR_NOMEM      = 4,   /* device or host allocation failed                       */
+  OIC_ERR_OVERFLOW   = 5,   /* a size limit of the engine was exceeded                */
+  OIC_ERR_STATE      = 6,   /* call out of order (e.g. no reads / no hash block)      */
+  OIC_ERR_DEVICE     = 7    /* a kernel reported an internal error flag               */
+};
+
+/* overlapInCore's parameters (overlapInCore.H:367-473; parsing overlapInCore.C:293-411).
+ * oic_default_params() gives the reference defaults. */
+typedef struct oic_params {
+  double      maxErate;          /* --maxerate; callers pass the strtof-rounded value     */
+  double      alignNoise;        /* --alignnoise (strtof-rounded)                          */
+  int32_t     partial;           /* -partial                                               */
+  int32_t     uniqueOlapPerPair; /* -u (1, default) or -m (0)                              */
+  int32_t     useHopelessCheck;  /* 0 after -z; the library also clears it when maxErate > 0.06 */
+  int32_t     minKmers;          /* --minkmers                                             */
+  uint32_t    kmerLen;           /* -k <int>, 1..31                                        */
+  uint32_t    hashBits;          /* --hashbits                                             */
+  double      maxHashLoad;       /* --hashload                                             */
+  uint64_t    maxHashDataLen;    /* --hashdatalen (the library adds AS_MAX_READLEN, overlapInCore.C:454) */
+  int32_t     minOlapLen;        /* --minlength                                            */
+  uint32_t    numThreads;        /* -t; only its effect on which ref reads a chunked run visits */
+  uint32_t    bgnHashID, endHashID, minLibToHash, maxLibToHash;   /* -h, -H               */
+  uint32_t    bgnRefID, endRefID, minLibToRef, maxLibToRef;       /* -r, -R               */
+} oic_params;
+
+/* The -s stats counters (overlapInCore.C:550-558) plus work counters. */
+typedef struct oic_stats {
+  uint64_t kmerHitsWithoutOlap, kmerHitsWithOlap, kmerHitsSkipped, multiOverlap;
+  uint64_t totalOverlaps, containedOverlaps, dovetailOverlaps;
+  uint64_t badShortWindow, badLongWindow;
+  uint64_t dpCells, slideBases, extensions, seeds, candidatePairs, nodes;
+  uint32_t nHashBlocks, reserved;
+  double   msHash, msSeed, msAlign, msTotal;       /* device time of the last oic_run */
+} oic_stats;
+
+typedef struct oic_ctx oic_ctx;
+
+/* Reference defaults (oicParameters::initialize, overlapInCore.H:374-411). */
+void oic_default_params(oic_params *p);
+
+/* Create a context on CUDA device `device`.  Replaces main()'s setup and
+ * Initialize_Work_Area (overlapInCore.C:113-144, 452-523): validates the parameters,
+ * builds the Edit_Match_Limit and Error_Bound tables (prefixEditDistance.C:23-90,
+ * Binomial_Bound.C:104-195) on the host and uploads them. */
+int  oic_create(const oic_params *p, int device, oic_ctx **out);
+void oic_destroy(oic_ctx *ctx);
+
+/* Load the read store: the 1-based read IDs 1..nReads with their library IDs,
+ * lengths and bases (A/C/G/T/N, either case) at bases[offset[i] .. offset[i]+length[i]).
+ * Replaces sqStore / sqCache_loadReads (overlapInCore.C:166-195).  Reads are packed
+ * to 2 bits per base (both strands) plus an N mask on the device. */
+int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const uint32_t *length,
+                  const uint64_t *offset, const char *bases, uint64_t nBases);
+
+/* Optional skip list: nKmers k-mers of exactly kmerLen bases each, concatenated
+ * (the -k <file> contents, Build_Hash_Index.C:184-257).  Each k-mer and its reverse
+ * complement are screened in every hash block built afterwards. */
+int oic_set_skip_kmers(oic_ctx *ctx, const char *kmers, uint64_t nKmers);
+
+/* Build one hash block starting at read bgnID and ending at or before endID
+ * (Build_Hash_Index, overlapInCore-Build_Hash_Index.C:414-631).  *lastLoaded gets the
+ * ID of the last read placed in the block. */
+int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *lastLoaded);
+
+/* Overlap every ref read of [bgnRefID, endRefID] (both strands) against the loaded
+ * block (Process_Overlaps / Find_Overlaps / Process_String_Olaps, overlapInCore-
+ * Process_Overlaps.C:24-122).  The records are appended to the context's output. */
+int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID);
+
+/* The whole stage (OverlapDriver, overlapInCore.C:161-277): every hash block of the
+ * -h range against the -r range, with the reference's range clamping and chunking
+ * rules.  Records are appended to the context's output. */
+int oic_run(oic_ctx *ctx);
+
+/* Number of records accumulated so far, and a copy of them (6 uint32 each) into
+ * `words` (capacity maxRecords).  oic_clear_overlaps() empties the output. */
+int oic_num_overlaps(oic_ctx *ctx, uint64_t *n);
+int oic_fetch_overlaps(oic_ctx *ctx, uint32_t *words, uint64_t maxRecords, uint64_t *n);
+int oic_clear_overlaps(oic_ctx *ctx);
+
+int oic_get_stats(oic_ctx *ctx, oic_stats *st);
+
+/* Batched Extend_Alignment (prefixEditDistance-extend.C:36-183) over nAlign
+ * independent problems, for direct testing of the DP kernel.  Problem i aligns the
+ * exact match (mStart[i] in S, mOffset[i] in T, mLen[i]) of S = read sRead[i] on
+ * strand sRev[i] (0 forward, 1 reverse complement) against T = read tRead[i]
+ * (forward), all 1-based IDs of the loaded store.  out[5*i .. 5*i+4] = S_Lo, S_Hi,
+ * T_Lo, T_Hi, Errors; kind[i] = 0 NONE, 1 LEFT_BRANCH_PT, 2 RIGHT_BRANCH_PT,
+ * 3 DOVETAIL; deltaLen[i] = merged Left_Delta length. */
+int oic_extend_batch(oic_ctx *ctx, uint32_t nAlign, const uint32_t *sRead, const uint32_t *sRev,
+                     const uint32_t *tRead, const int32_t *mStart, const int32_t *mOffset,
+                     const int32_t *mLen, int32_t *out, int32_t *kind, int32_t *deltaLen);
+
+/* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
+ * min(n, table length) entries; *len gets the table length. */
+int oic_get_match_limit(oic_ctx *ctx, int32_t *dst, uint32_t n, uint32_t *len);
+
+/* Last CUDA / kernel error text of the context (never NULL). */
+const char *oic_last_error(oic_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
