@@ -57,7 +57,7 @@ class OicStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "kmerHitsWithoutOlap", "kmerHitsWithOlap", "kmerHitsSkipped", "multiOverlap",
         "totalOverlaps", "containedOverlaps", "dovetailOverlaps", "badShortWindow", "badLongWindow",
-        "dpCells", "slideBases", "extensions", "seeds", "candidatePairs", "nodes")] + [
+        "dpCells", "slideBases", "extensions", "seeds", "candidatePairs", "nodes", "dpRows")] + [
         ("nHashBlocks", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
         ("msHash", ctypes.c_double), ("msSeed", ctypes.c_double),
         ("msAlign", ctypes.c_double), ("msTotal", ctypes.c_double)]

@@ -18,9 +18,7 @@ namespace oic {
 // Per-warp global scratch.
 struct WarpScratch {
   int  *arena;       // kept DP rows, band-compacted
-  int  *rowOff;      // per error row: arena offset
-  int  *rowL;        // per error row: kept band [rowL, rowR]
-  int  *rowR;
+  int4 *rowHdr;      // per error row: (arena offset, kept band left, kept band right, unused)
   int  *deltaL;      // Left_Delta (merged delta of the last extension)
   int  *deltaR;      // Right_Delta
   int  *stack;       // Delta_Stack
@@ -40,7 +38,7 @@ struct WarpDP {
   int               *smA, *smB;     // shared-memory row buffers (bandW ints each)
   const int         *eml;           // Edit_Match_Limit
   DevParams          P;
-  unsigned long long cells, slides;
+  unsigned long long cells, slides, rows;
   u32                err;           // capacity error of the current pair (0 = ok)
   int                leftLen, rightLen;
 };
@@ -73,10 +71,11 @@ __device__ __forceinline__ int warp_slide0(const SeqView &A, i64 a0, const SeqVi
 // Traceback of Set_Right_Delta / Set_Left_Delta (prefixEditDistance-forward.C:32-71,
 // -reverse.C:36-93) from row e, diagonal d whose value is `last`.  Lane 0 only.
 // Pushes one entry per indel into out[]; returns the value reached on row 0.
-__device__ __forceinline__ int trace_rows(const WarpDP &w, int e, int d, int last, int *out, int &n) {
+static __device__ __noinline__ int trace_rows(const WarpDP &w, int e, int d, int last, int *out, int &n) {
   n = 0;
   for (int k = e; k > 0; k--) {
-    const int off = w.sc.rowOff[k - 1], L = w.sc.rowL[k - 1], R = w.sc.rowR[k - 1];
+    const int4 h = w.sc.rowHdr[k - 1];
+    const int off = h.x, L = h.y, R = h.z;
     const int g0 = (d >= L && d <= R) ? w.sc.arena[off + d - L] : -2;
     const int gm = (d - 1 >= L && d - 1 <= R) ? w.sc.arena[off + d - 1 - L] : -2;
     const int gp = (d + 1 >= L && d + 1 <= R) ? w.sc.arena[off + d + 1 - L] : -2;
@@ -97,12 +96,12 @@ __device__ __forceinline__ int trace_rows(const WarpDP &w, int e, int d, int las
 }
 
 __device__ __forceinline__ int arena_get(const WarpDP &w, int e, int d) {
-  const int L = w.sc.rowL[e], R = w.sc.rowR[e];
-  return (d >= L && d <= R) ? w.sc.arena[w.sc.rowOff[e] + d - L] : -2;
+  const int4 h = w.sc.rowHdr[e];
+  return (d >= h.y && d <= h.z) ? w.sc.arena[h.x + d - h.y] : -2;
 }
 
 // Set_Right_Delta (forward.C:32-71) into sc.deltaR; lane 0.
-__device__ __forceinline__ void set_right_delta(WarpDP &w, int e, int d, int last) {
+static __device__ __noinline__ void set_right_delta(WarpDP &w, int e, int d, int last) {
   int n;
   int l = trace_rows(w, e, d, last, w.sc.stack, n);
   w.sc.stack[n++] = l + 1;
@@ -115,7 +114,7 @@ __device__ __forceinline__ void set_right_delta(WarpDP &w, int e, int d, int las
 }
 
 // Set_Left_Delta (reverse.C:36-93) into sc.deltaL; lane 0.
-__device__ __forceinline__ void set_left_delta(WarpDP &w, int e, int d, int last, int &leftover, int &tEnd, int tLen) {
+static __device__ __noinline__ void set_left_delta(WarpDP &w, int e, int d, int last, int &leftover, int &tEnd, int tLen) {
   int n;
   leftover  = trace_rows(w, e, d, last, w.sc.deltaL, n);
   int *ld   = w.sc.deltaL;
@@ -134,7 +133,7 @@ __device__ __forceinline__ void set_left_delta(WarpDP &w, int e, int d, int last
 // A[STEP*i] is base a0+STEP*i of view A, T likewise.  Returns the error count; the
 // outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
 template <int STEP>
-__device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
+static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
                               int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
   const int lane = threadIdx.x & 31;
   const double BMV = w.P.branchMatchValue;
@@ -152,12 +151,13 @@ __device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const 
 
   if (lane == 0) {
     w.sc.arena[0]  = r0;
-    w.sc.rowOff[0] = 0;
-    w.sc.rowL[0]   = 0;
-    w.sc.rowR[0]   = 0;
+    w.sc.rowHdr[0] = make_int4(0, 0, 0, 0);
   }
+  // Row buffers hold diagonal d at index d - base + 2.  Before a row is computed the
+  // two diagonals on each side of the previous row's kept band are set to -2, as the
+  // reference does (forward.C:150-153), so the neighbour reads need no bounds tests.
   int *prev = w.smA, *cur = w.smB;
-  if (lane == 0) prev[0] = r0;
+  if (lane == 0) prev[2] = r0;
   __syncwarp();
 
   int    used = 1, prevBase = 0, L = 0, R = 0;
@@ -169,27 +169,36 @@ __device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const 
     if (e >= w.cap.rowCap) { w.err |= kErrRowsFull; return 0; }
     const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
     const int width = Rc - Lc + 1;
-    if (width > w.cap.bandW) { w.err |= kErrBandWide; return 0; }
+    if (width + 4 > w.cap.bandW) { w.err |= kErrBandWide; return 0; }
 
-    int myEnd = INT_MAX;
+    const int lim = w.eml[e];
+    if (lane < 4) prev[(lane < 2 ? L - 2 + lane : R - 1 + lane) - prevBase + 2] = -2;
+    __syncwarp();
+    const int *pv = prev + (2 - prevBase);   // pv[d] = row e-1 at diagonal d
+    int       *cv = cur + (2 - Lc);          // cv[d] = row e at diagonal d
+    int myEnd = INT_MAX, myL = INT_MAX, myR = INT_MIN;
     for (int d = Lc + lane; d <= Rc; d += 32) {
-      const int p0 = (d >= L && d <= R) ? prev[d - prevBase] : -2;
-      const int pm = (d - 1 >= L && d - 1 <= R) ? prev[d - 1 - prevBase] : -2;
-      const int pp = (d + 1 >= L && d + 1 <= R) ? prev[d + 1 - prevBase] : -2;
+      const int p0 = pv[d], pm = pv[d - 1], pp = pv[d + 1];
       int row = 1 + p0;
       if (pm > row) row = pm;
       if (1 + pp > row) row = 1 + pp;
-      const int lim = min(m - row, n - row - d);
-      if (lim > 0) row += slide<STEP>(A, a0, T, t0, row, d, lim, w.slides);
-      cur[d - Lc] = row;
+      const int room = min(m - row, n - row - d);
+      if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, w.slides);
+      cv[d] = row;
       if ((row == m || row + d == n) && d < myEnd) myEnd = d;
+      // pruneAlign (prefixEditDistance.H:249-258): extra = max(d, 0) on both band edges
+      if (!(row + max(d, 0) < lim)) {
+        if (myL == INT_MAX) myL = d;
+        myR = d;
+      }
     }
     __syncwarp();
-    const int dEnd = warp_min(myEnd);
+    w.rows++;
+    const int dEnd = __reduce_min_sync(0xffffffffu, myEnd);
 
     if (dEnd != INT_MAX) {
       w.cells += (unsigned long long)(dEnd - Lc + 1);
-      const int    row     = cur[dEnd - Lc];
+      const int    row     = cv[dEnd];
       const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
       const int    tailLen = row - msLen;
       const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
@@ -216,8 +225,7 @@ __device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const 
       int d = dEnd;
       if (STEP > 0) {
         // Force the last error to be a mismatch (forward.C:215-221).
-        const int pp = (d + 1 >= L && d + 1 <= R) ? prev[d + 1 - prevBase] : -2;
-        if (row == m && 1 + pp == row && d < Rc) d++;
+        if (row == m && 1 + pv[d + 1] == row && d < Rc) d++;
         aEnd = row;
         tEnd = row + d;
         if (lane == 0) set_right_delta(w, e, d, row);
@@ -236,50 +244,38 @@ __device__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const 
     }
     w.cells += (unsigned long long)width;
 
-    // Band pruning (forward.C:245-280): the kept band is [first, last] unpruned diagonal.
-    const int lim = w.eml[e];
-    int myL = INT_MAX, myR = INT_MIN;
-    for (int d = Lc + lane; d <= Rc; d += 32) {
-      const int v = cur[d - Lc];
-      if (!(v + max(d, 0) < lim)) {
-        myL = min(myL, d);
-        myR = max(myR, d);
-      }
-    }
-    const int L2 = warp_min(myL);
+    // The kept band is [first, last] unpruned diagonal (forward.C:245-280).
+    const int L2 = __reduce_min_sync(0xffffffffu, myL);
     if (L2 == INT_MAX) break;
-    const int R2 = warp_max(myR);
+    const int R2 = __reduce_max_sync(0xffffffffu, myR);
 
     // Longest row on the kept band, first diagonal on ties (forward.C:284-289).
     int myV = -1, myD = INT_MAX;
     for (int d = L2 + lane; d <= R2; d += 32) {
-      const int v = cur[d - Lc];
+      const int v = cv[d];
       if (v > myV) { myV = v; myD = d; }
     }
-    const int rowMax = warp_max(myV);
-    const int dMax   = warp_min(myV == rowMax ? myD : INT_MAX);
+    const int rowMax = __reduce_max_sync(0xffffffffu, myV);
     if (rowMax > longest) {
       longest = rowMax;
-      bestD   = dMax;
+      bestD   = __reduce_min_sync(0xffffffffu, myV == rowMax ? myD : INT_MAX);
       bestE   = e;
-    }
-    const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
-    if (score > maxScore) {
-      maxScore = score;
-      msLen    = longest;
-      msD      = bestD;
-      msE      = bestE;
+      // Score only moves up when Longest does: with Longest unchanged, rounding is
+      // monotone, so Longest*BMV - e cannot pass the Max_Score of an earlier row.
+      const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
+      if (score > maxScore) {
+        maxScore = score;
+        msLen    = longest;
+        msD      = bestD;
+        msE      = bestE;
+      }
     }
 
     // Keep the band for the traceback.
     const int cnt = R2 - L2 + 1;
     if (used + cnt > w.cap.arenaCap) { w.err |= kErrArenaFull; return 0; }
-    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cur[d - Lc];
-    if (lane == 0) {
-      w.sc.rowOff[e] = used;
-      w.sc.rowL[e]   = L2;
-      w.sc.rowR[e]   = R2;
-    }
+    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cv[d];
+    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, 0);
     used += cnt;
     int *t = prev;
     prev   = cur;
@@ -314,7 +310,7 @@ enum { kNone = 0, kLeftBranch = 1, kRightBranch = 2, kDovetail = 3 };
 
 // Extend_Alignment (prefixEditDistance-extend.C:36-183), one warp.  The merged delta
 // ends up in sc.deltaL[0 .. leftLen).  Outputs are warp-uniform.
-__device__ inline int warp_extend(WarpDP &w, const SeqView &S, int sLen, const SeqView &T, int tLen, int mStart,
+static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int sLen, const SeqView &T, int tLen, int mStart,
                            int mOffset, int mLen, int &sLo, int &sHi, int &tLo, int &tHi, int &errors) {
   const int lane = threadIdx.x & 31;
   int  rightErrors = 0, leftErrors = 0, leftover = 0;

@@ -141,9 +141,9 @@ struct oic_ctx {
   uint32_t pairCap = 0, nodeCap = 0;
 
   // align
-  DevBuf dWork, dRec, dCnt, dRecPos, dRecOut, dAlnOvf;
-  DevBuf dArena, dRowOff, dRowL, dRowR, dDL, dDR, dStack, dAlive;           // normal
-  DevBuf dArena2, dRowOff2, dRowL2, dRowR2, dDL2, dDR2, dStack2, dAlive2;   // wide
+  DevBuf dWork, dRec, dCnt, dRecPos, dRecOut, dAlnOvf, dWorkK, dWorkK2, dWorkV2, dWorkScratch;
+  DevBuf dArena, dRowHdr, dDL, dDR, dStack, dAlive;        // normal
+  DevBuf dArena2, dRowHdr2, dDL2, dDR2, dStack2, dAlive2;  // wide
   DevBuf dScanScratch;
 
   // counters (one small device block): [0..15] u32 counters, [16..] u64 stats
@@ -242,12 +242,12 @@ struct AlignConfig {
 
 AlignConfig align_normal(const oic_ctx *c) {
   AlignConfig a;
-  a.bandW         = 1024;
-  a.warps         = c->nSM * 3 * align_warps_per_block(1024);
+  a.bandW         = 512;
+  a.warps         = c->nSM * 3 * align_warps_per_block(512);
   a.caps.arenaCap = 1 << 19;
   a.caps.rowCap   = 1 << 14;
   a.caps.nodeCap  = 1 << 16;
-  a.caps.bandW    = 1024;
+  a.caps.bandW    = 512;
   return a;
 }
 AlignConfig align_wide(const oic_ctx *c) {
@@ -264,25 +264,19 @@ AlignConfig align_wide(const oic_ctx *c) {
 int ensure_align_scratch(oic_ctx *ctx, const AlignConfig &ac, bool wide, WarpScratch &s) {
   const size_t W = (size_t)ac.warps;
   DevBuf &ar = wide ? ctx->dArena2 : ctx->dArena;
-  DevBuf &ro = wide ? ctx->dRowOff2 : ctx->dRowOff;
-  DevBuf &rl = wide ? ctx->dRowL2 : ctx->dRowL;
-  DevBuf &rr = wide ? ctx->dRowR2 : ctx->dRowR;
+  DevBuf &rh = wide ? ctx->dRowHdr2 : ctx->dRowHdr;
   DevBuf &dl = wide ? ctx->dDL2 : ctx->dDL;
   DevBuf &dr = wide ? ctx->dDR2 : ctx->dDR;
   DevBuf &sk = wide ? ctx->dStack2 : ctx->dStack;
   DevBuf &al = wide ? ctx->dAlive2 : ctx->dAlive;
   CK(ar.ensure(W * ac.caps.arenaCap * sizeof(int)));
-  CK(ro.ensure(W * ac.caps.rowCap * sizeof(int)));
-  CK(rl.ensure(W * ac.caps.rowCap * sizeof(int)));
-  CK(rr.ensure(W * ac.caps.rowCap * sizeof(int)));
+  CK(rh.ensure(W * ac.caps.rowCap * sizeof(int4)));
   CK(dl.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(dr.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(sk.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(al.ensure(W * ac.caps.nodeCap));
   s.arena  = ar.as<int>();
-  s.rowOff = ro.as<int>();
-  s.rowL   = rl.as<int>();
-  s.rowR   = rr.as<int>();
+  s.rowHdr = rh.as<int4>();
   s.deltaL = dl.as<int>();
   s.deltaR = dr.as<int>();
   s.stack  = sk.as<int>();
@@ -380,11 +374,15 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   CK(ctx->dRecPos.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
   CK(ctx->dRec.ensure((size_t)std::max<uint32_t>(nPairs, 1) * 18 * sizeof(uint32_t)));
   CK(ctx->dAlnOvf.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
-  {
-    std::vector<uint32_t> work(nPairs);
-    for (uint32_t i = 0; i < nPairs; i++) work[i] = i;
-    if (nPairs) CK(cudaMemcpyAsync(ctx->dWork.p, work.data(), nPairs * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
+  if (nPairs) {
+    // Pairs with the most match nodes (the most extensions) go first.
+    CK(ctx->dWorkK.ensure((size_t)nPairs * 8));
+    CK(ctx->dWorkK2.ensure((size_t)nPairs * 8));
+    CK(ctx->dWorkV2.ensure((size_t)nPairs * 4));
+    CK(ctx->dWorkScratch.ensure(radix_sort_scratch(nPairs) + 256));
+    launch_work_keys(ctx->dPairs.as<PairRec>(), nPairs, ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->st);
+    CK(radix_sort_u64_u32(ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->dWorkK2.as<u64>(),
+                          ctx->dWorkV2.as<uint32_t>(), nPairs, 32, ctx->dWorkScratch.p, ctx->st));
   }
   if (nPairs) CK(cudaMemsetAsync(ctx->dCnt.p, 0, nPairs * sizeof(uint32_t), ctx->st));
   AlignOut ao;
@@ -466,6 +464,7 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   S.dpCells += st64[2 + kStCells];
   S.slideBases += st64[2 + kStSlides];
   S.extensions += st64[2 + kStExtensions];
+  S.dpRows += st64[2 + kStRows];
   return OIC_OK;
 }
 
@@ -569,10 +568,11 @@ void oic_destroy(oic_ctx *ctx) {
                     &ctx->dNodes,    &ctx->dSegOvf,     &ctx->dSeedSlotK,  &ctx->dSeedSlotV, &ctx->dSeedPairs,
                     &ctx->dSeedNodes, &ctx->dSeedSlotK2, &ctx->dSeedSlotV2, &ctx->dSeedPairs2, &ctx->dSeedNodes2,
                     &ctx->dWork,     &ctx->dRec,        &ctx->dCnt,        &ctx->dRecPos,    &ctx->dRecOut,
-                    &ctx->dAlnOvf,   &ctx->dArena,      &ctx->dRowOff,     &ctx->dRowL,      &ctx->dRowR,
+                    &ctx->dAlnOvf,   &ctx->dArena,      &ctx->dRowHdr,
                     &ctx->dDL,       &ctx->dDR,         &ctx->dStack,      &ctx->dAlive,     &ctx->dArena2,
-                    &ctx->dRowOff2,  &ctx->dRowL2,      &ctx->dRowR2,      &ctx->dDL2,       &ctx->dDR2,
-                    &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr};
+                    &ctx->dRowHdr2,  &ctx->dDL2,       &ctx->dDR2,
+                    &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr,
+                    &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch};
   for (DevBuf *b : bufs) b->release();
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;

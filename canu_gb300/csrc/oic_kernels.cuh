@@ -92,10 +92,10 @@ struct AlignOut {
 
 enum StatIdx {
   kStWithoutOlap = 0, kStWithOlap, kStSkipped, kStMulti, kStTotal, kStContained, kStDovetail,
-  kStCells, kStSlides, kStExtensions, kStCount
+  kStCells, kStSlides, kStExtensions, kStRows, kStCount
 };
 
-// bandW selects the shared-memory configuration (compiled instances: 1024, 8192).
+// bandW selects the shared-memory configuration (compiled instances: 512, 8192).
 void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs,
                   const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap,
                   int nWarps, AlignOut out, cudaStream_t st);
@@ -107,6 +107,9 @@ struct ExtendProblem {
 void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
                          WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
                          unsigned long long *stats, cudaStream_t st);
+
+// Sort keys that put the pairs with the most match nodes first.
+void launch_work_keys(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals, cudaStream_t st);
 
 // Compact per-pair record slots into a dense record array.
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st);

@@ -19,7 +19,7 @@ namespace oic {
 
 namespace {
 
-constexpr int kAlignWarpsSmall = 8;   // bandW 1024
+constexpr int kAlignWarpsSmall = 8;   // bandW 512
 constexpr int kAlignWarpsLarge = 1;   // bandW 8192
 
 struct Olap {
@@ -177,6 +177,14 @@ struct PairCounts {
   unsigned long long v[kStCount];
 };
 
+// Per-warp shared state of the pair driver (kept out of registers).
+struct PairSmem {
+  Olap               olap[kMaxDistinct];
+  int                nOlap;
+  PairCounts         pc;    // counts of the pair in flight
+  PairCounts         acc;   // committed counts of the warp
+};
+
 // Output_Overlap (Output.C:26-191).
 __device__ void output_overlap(u32 *dst, u32 sID, int sLen, int rev, u32 tID, int tLen, const Olap &o,
                                PairCounts &pc) {
@@ -233,9 +241,7 @@ __device__ void output_partial(u32 *dst, u32 sID, u32 tID, int rev, const Olap &
 __device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &base, const AlignCaps &cap, u64 gw) {
   WarpScratch s;
   s.arena  = base.arena + gw * (u64)cap.arenaCap;
-  s.rowOff = base.rowOff + gw * (u64)cap.rowCap;
-  s.rowL   = base.rowL + gw * (u64)cap.rowCap;
-  s.rowR   = base.rowR + gw * (u64)cap.rowCap;
+  s.rowHdr = base.rowHdr + gw * (u64)cap.rowCap;
   s.deltaL = base.deltaL + gw * (u64)(cap.rowCap + 8);
   s.deltaR = base.deltaR + gw * (u64)(cap.rowCap + 8);
   s.stack  = base.stack + gw * (u64)(cap.rowCap + 8);
@@ -243,29 +249,27 @@ __device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &base, con
   return s;
 }
 
-// Process_Matches for one pair.  Returns false on a capacity overflow (nothing was
-// written, pc untouched).
-__device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, const PairRec &pr, const int4 *nodesAll,
-                             u32 *recOut, u32 &nRec, PairCounts &pcOut) {
+// Process_Matches for one pair.  Counts go to ps.pc, records (lane 0) to recOut.
+// Returns false on a capacity overflow: the caller then discards ps.pc and the records.
+__device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const TableDev &Tb, const PairRec &pr,
+                             const int4 *nodesAll, u32 *recOut, u32 &nRec) {
   const int lane = threadIdx.x & 31;
   const DevParams &P = w.P;
-  PairCounts pc;
+  if (lane == 0) {
 #pragma unroll
-  for (int i = 0; i < kStCount; i++) pc.v[i] = 0;
+    for (int i = 0; i < kStCount; i++) ps.pc.v[i] = 0;
+    ps.nOlap = 0;
+  }
+  __syncwarp();
   nRec = 0;
 
   const u32 sRead = pr.sRead;
   const int rev   = pr.flags & 1;
   const int cons  = (pr.flags >> 1) & 1;
   const bool segL = (pr.flags >> 2) & 1, segR = (pr.flags >> 3) & 1;
-  const SeqView S = make_view(R, sRead, rev);
   const int sLen  = (int)R.len[sRead];
-  const u32 sID   = sRead + 1;
   const u32 tRead = Tb.sread[pr.tStr];
-  const SeqView T = make_view(R, tRead, 0);
   const int tLen  = (int)R.len[tRead];
-  const u32 tID   = tRead + 1;
-  const bool tLs = Tb.lscr[pr.tStr] != 0, tRs = Tb.rscr[pr.tStr] != 0;
 
   // --minkmers (computeMinimumKmers, Process_String_Overlaps.C:21-33, :618-621)
   if (P.minKmers) {
@@ -273,11 +277,12 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
     if (ol < 0) ol = -ol;
     unsigned long long ex = 0;
     if (!(ol < (double)P.kmerLen))
-      ex = (unsigned long long)(long long)(int)floor(__dmul_rn(P.kmerExpect, __dadd_rn(__dsub_rn(ol, (double)P.kmerLen), 1.0)));
+      ex = (unsigned long long)(long long)(int)floor(
+          __dmul_rn(P.kmerExpect, __dadd_rn(__dsub_rn(ol, (double)P.kmerLen), 1.0)));
     const unsigned long long need = P.minKmers > ex ? P.minKmers : ex;
     if (need > (unsigned long long)(long long)pr.diagCt) {
-      pc.v[kStSkipped]++;
-      pcOut = pc;
+      if (lane == 0) ps.pc.v[kStSkipped] = 1;
+      __syncwarp();
       return true;
     }
   }
@@ -285,14 +290,15 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
   const int4 *nodes = nodesAll + pr.nodeOff;
   const int   cnt   = (int)pr.nodeCnt;
   if (cnt <= 0) {
-    pc.v[kStWithoutOlap]++;
-    pcOut = pc;
+    if (lane == 0) ps.pc.v[kStWithoutOlap] = 1;
+    __syncwarp();
     return true;
   }
 
   // Hopeless check for a single match (:384-415).
   if (P.hopeless && cnt == 1 && !P.partial) {
     const int4 m = nodes[0];   // x offset, y len, z start
+    const bool tLs = Tb.lscr[pr.tStr] != 0, tRs = Tb.rscr[pr.tStr] != 0;
     bool hopeless = false;
     const int sHead = m.z, tHead = m.x;
     if (sHead <= tHead) {
@@ -307,8 +313,8 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
       if (tTail > kHopelessMatch && !tRs) hopeless = true;
     }
     if (hopeless) {
-      pc.v[kStWithoutOlap]++;
-      pcOut = pc;
+      if (lane == 0) ps.pc.v[kStWithoutOlap] = 1;
+      __syncwarp();
       return true;
     }
   }
@@ -320,21 +326,24 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
   for (int i = lane; i < cnt; i += 32) w.sc.alive[i] = 1;
   __syncwarp();
 
-  Olap olap[kMaxDistinct];
-  int  nOlap = 0;
-  const unsigned long long cells0 = w.cells, slides0 = w.slides;
+  const SeqView S = make_view(R, sRead, rev);
+  const SeqView T = make_view(R, tRead, 0);
+  const unsigned long long cells0 = w.cells, slides0 = w.slides, rows0 = w.rows;
 
   while (true) {
     // Longest remaining match, first in list order on ties (:424-431).
     int myLen = -1, myIdx = INT_MAX;
     for (int i = lane; i < cnt; i += 32)
-      if (w.sc.alive[i] && nodes[i].y > myLen) {
-        myLen = nodes[i].y;
-        myIdx = i;
+      if (w.sc.alive[i]) {
+        const int len = nodes[i].y;
+        if (len > myLen) {
+          myLen = len;
+          myIdx = i;
+        }
       }
-    const int maxLen = warp_max(myLen);
+    const int maxLen = __reduce_max_sync(0xffffffffu, myLen);
     if (maxLen < 0) break;
-    const int li = warp_min(myLen == maxLen ? myIdx : INT_MAX);
+    const int li = __reduce_min_sync(0xffffffffu, myLen == maxLen ? myIdx : INT_MAX);
     const int4 lm = nodes[li];
 
     int sLo = 0, sHi = 0, tLo = 0, tHi = 0, errors = 0;
@@ -342,16 +351,18 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
     if (w.err) {
       w.cells  = cells0;
       w.slides = slides0;
+      w.rows   = rows0;
       return false;
     }
-    pc.v[kStExtensions]++;
-
     const bool dov = (kind == kDovetail) || P.partial;
-    if (dov && 1 + sHi - sLo >= P.minOlapLen && 1 + tHi - tLo >= P.minOlapLen) {
-      const int    olapLen = 1 + min(sHi - sLo, tHi - tLo);
-      const double quality = __ddiv_rn((double)errors, (double)olapLen);
-      if (errors <= error_bound(olapLen, P.maxErate))
-        add_overlap(P.partial, sLo, sHi, tLo, tHi, quality, w.leftLen, olap, nOlap);
+    if (lane == 0) {
+      ps.pc.v[kStExtensions]++;
+      if (dov && 1 + sHi - sLo >= P.minOlapLen && 1 + tHi - tLo >= P.minOlapLen) {
+        const int    olapLen = 1 + min(sHi - sLo, tHi - tLo);
+        const double quality = __ddiv_rn((double)errors, (double)olapLen);
+        if (errors <= error_bound(olapLen, P.maxErate))
+          add_overlap(P.partial, sLo, sHi, tLo, tHi, quality, w.leftLen, ps.olap, ps.nOlap);
+      }
     }
     if (cons) break;
 
@@ -368,43 +379,46 @@ __device__ bool process_pair(WarpDP &w, const ReadsDev &R, const TableDev &Tb, c
     __syncwarp();
   }
 
-  int nOut = 0;
-  if (nOlap > 0) {
-    int deleted[kMaxDistinct] = {0, 0, 0};
-    if (P.partial) {
-      if (P.unique) choose_best_partial(olap, nOlap, deleted);
-    } else {
-      if (P.unique) combine_into_one(olap, nOlap, deleted);
-      else merge_intersecting(olap, nOlap, deleted);
-    }
-    for (int i = 0; i < nOlap; i++)
-      if (!deleted[i]) {
-        u32 rec[6];
-        if (P.partial) output_partial(rec, sID, tID, rev, olap[i], sLen, tLen, pc);
-        else output_overlap(rec, sID, sLen, rev, tID, tLen, olap[i], pc);
-        if (lane == 0)
-          for (int k = 0; k < 6; k++) recOut[nOut * 6 + k] = rec[k];
-        nOut++;
+  if (lane == 0) {
+    const u32 sID = sRead + 1, tID = tRead + 1;
+    int nOut = 0;
+    const int nOlap = ps.nOlap;
+    if (nOlap > 0) {
+      int deleted[kMaxDistinct] = {0, 0, 0};
+      if (P.partial) {
+        if (P.unique) choose_best_partial(ps.olap, nOlap, deleted);
+      } else {
+        if (P.unique) combine_into_one(ps.olap, nOlap, deleted);
+        else merge_intersecting(ps.olap, nOlap, deleted);
       }
+      for (int i = 0; i < nOlap; i++)
+        if (!deleted[i]) {
+          if (P.partial) output_partial(recOut + nOut * 6, sID, tID, rev, ps.olap[i], sLen, tLen, ps.pc);
+          else output_overlap(recOut + nOut * 6, sID, sLen, rev, tID, tLen, ps.olap[i], ps.pc);
+          nOut++;
+        }
+    }
+    if (nOut == 0) ps.pc.v[kStWithoutOlap]++;
+    else {
+      ps.pc.v[kStWithOlap]++;
+      if (nOut > 1) ps.pc.v[kStMulti]++;
+    }
+    nRec = (u32)nOut;
   }
-  if (nOut == 0) pc.v[kStWithoutOlap]++;
-  else {
-    pc.v[kStWithOlap]++;
-    if (nOut > 1) pc.v[kStMulti]++;
-  }
-  nRec  = (u32)nOut;
-  pcOut = pc;
+  __syncwarp();
   return true;
 }
 
 template <int BANDW, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
+__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
                                                            const PairRec *pairs, const u32 *work, u32 nWork,
                                                            u32 *workCounter, const int4 *nodes, WarpScratch scBase,
                                                            AlignCaps cap, AlignOut out) {
   extern __shared__ int smemRows[];
+  __shared__ PairSmem pairSmem[WARPS];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const u64 gw   = (u64)blockIdx.x * WARPS + wib;
+  PairSmem &ps   = pairSmem[wib];
 
   WarpDP w;
   w.sc     = warp_scratch(scBase, cap, gw);
@@ -415,12 +429,12 @@ __global__ void __launch_bounds__(WARPS * 32) align_kernel(ReadsDev R, TableDev 
   w.P      = P;
   w.cells  = 0;
   w.slides = 0;
+  w.rows   = 0;
   w.err    = 0;
   w.leftLen = w.rightLen = 0;
-
-  PairCounts acc;
-#pragma unroll
-  for (int i = 0; i < kStCount; i++) acc.v[i] = 0;
+  if (lane == 0)
+    for (int i = 0; i < kStCount; i++) ps.acc.v[i] = 0;
+  __syncwarp();
 
   while (true) {
     u32 k = 0;
@@ -430,15 +444,13 @@ __global__ void __launch_bounds__(WARPS * 32) align_kernel(ReadsDev R, TableDev 
     const u32 pi = work[k];
     const PairRec pr = pairs[pi];
     u32 nRec = 0;
-    PairCounts pc;
     w.err = 0;
-    const bool ok = process_pair(w, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, pc);
-    if (ok) {
-      if (lane == 0) out.cnt[pi] = nRec;
-#pragma unroll
-      for (int i = 0; i < kStCount; i++) acc.v[i] += pc.v[i];
-    } else {
-      if (lane == 0) {
+    const bool ok = process_pair(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec);
+    if (lane == 0) {
+      if (ok) {
+        out.cnt[pi] = nRec;
+        for (int i = 0; i < kStCount; i++) ps.acc.v[i] += ps.pc.v[i];
+      } else {
         out.cnt[pi] = 0;
         u32 slot = atomicAdd(out.overflowCount, 1u);
         out.overflow[slot] = pi;
@@ -447,19 +459,19 @@ __global__ void __launch_bounds__(WARPS * 32) align_kernel(ReadsDev R, TableDev 
     }
     __syncwarp();
   }
-  // Cells are warp-uniform; slides are counted per lane.
+  // Cells and rows are warp-uniform; slides are counted per lane.
   const unsigned long long slidesWarp = warp_sum64(w.slides);
   if (lane == 0) {
-    acc.v[kStCells] += w.cells;
-    acc.v[kStSlides] += slidesWarp;
-#pragma unroll
+    ps.acc.v[kStCells] += w.cells;
+    ps.acc.v[kStSlides] += slidesWarp;
+    ps.acc.v[kStRows] += w.rows;
     for (int i = 0; i < kStCount; i++)
-      if (acc.v[i]) atomicAdd(&out.stats[i], acc.v[i]);
+      if (ps.acc.v[i]) atomicAdd(&out.stats[i], ps.acc.v[i]);
   }
 }
 
 template <int BANDW, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) extend_batch_kernel(ReadsDev R, DevParams P, const int *eml,
+__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) extend_batch_kernel(ReadsDev R, DevParams P, const int *eml,
                                                                   const ExtendProblem *probs, u32 n, WarpScratch scBase,
                                                                   AlignCaps cap, int *out, int *kind, int *deltaLen,
                                                                   u32 *status, unsigned long long *stats) {
@@ -477,6 +489,7 @@ __global__ void __launch_bounds__(WARPS * 32) extend_batch_kernel(ReadsDev R, De
   w.P      = P;
   w.cells  = 0;
   w.slides = 0;
+  w.rows   = 0;
   w.err    = 0;
   w.leftLen = w.rightLen = 0;
 
@@ -507,6 +520,14 @@ __global__ void __launch_bounds__(WARPS * 32) extend_batch_kernel(ReadsDev R, De
   }
 }
 
+// Longest work first: key = ~(match nodes of the pair), value = pair index.
+__global__ void work_keys_kernel(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals) {
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    keys[i] = 0xffffffffull - (unsigned long long)pairs[i].nodeCnt;
+    vals[i] = i;
+  }
+}
+
 __global__ void compact_records_kernel(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst) {
   for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p < nPairs; p += gridDim.x * blockDim.x) {
     const u32 c = cnt[p];
@@ -516,10 +537,10 @@ __global__ void compact_records_kernel(const u32 *rec, const u32 *cnt, const u32
 
 }  // namespace
 
-int align_warps_per_block(int bandW) { return bandW <= 1024 ? kAlignWarpsSmall : kAlignWarpsLarge; }
+int align_warps_per_block(int bandW) { return bandW <= 512 ? kAlignWarpsSmall : kAlignWarpsLarge; }
 
 size_t align_smem_bytes(int bandW) {
-  const int b = bandW <= 1024 ? 1024 : 8192;
+  const int b = bandW <= 512 ? 512 : 8192;
   return (size_t)align_warps_per_block(bandW) * 2 * b * sizeof(int);
 }
 
@@ -530,9 +551,9 @@ void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml
   const int wpb = align_warps_per_block(bandW);
   const int blocks = (nWarps + wpb - 1) / wpb;
   const size_t smem = align_smem_bytes(bandW);
-  cap.bandW = bandW <= 1024 ? 1024 : 8192;
-  if (bandW <= 1024) {
-    auto k = align_kernel<1024, kAlignWarpsSmall>;
+  cap.bandW = bandW <= 512 ? 512 : 8192;
+  if (bandW <= 512) {
+    auto k = align_kernel<512, kAlignWarpsSmall>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
   } else {
@@ -549,9 +570,9 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
   const int wpb = align_warps_per_block(bandW);
   const int blocks = (nWarps + wpb - 1) / wpb;
   const size_t smem = align_smem_bytes(bandW);
-  cap.bandW = bandW <= 1024 ? 1024 : 8192;
-  if (bandW <= 1024) {
-    auto k = extend_batch_kernel<1024, kAlignWarpsSmall>;
+  cap.bandW = bandW <= 512 ? 512 : 8192;
+  if (bandW <= 512) {
+    auto k = extend_batch_kernel<512, kAlignWarpsSmall>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
   } else {
@@ -559,6 +580,13 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
   }
+}
+
+void launch_work_keys(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals, cudaStream_t st) {
+  if (n == 0) return;
+  unsigned g = (n + 255) / 256;
+  if (g > 65535u * 8) g = 65535u * 8;
+  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, keys, vals);
 }
 
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st) {

@@ -62,7 +62,7 @@ typedef struct oic_stats {
   uint64_t kmerHitsWithoutOlap, kmerHitsWithOlap, kmerHitsSkipped, multiOverlap;
   uint64_t totalOverlaps, containedOverlaps, dovetailOverlaps;
   uint64_t badShortWindow, badLongWindow;
-  uint64_t dpCells, slideBases, extensions, seeds, candidatePairs, nodes;
+  uint64_t dpCells, slideBases, extensions, seeds, candidatePairs, nodes, dpRows;
   uint32_t nHashBlocks, reserved;
   double   msHash, msSeed, msAlign, msTotal;       /* device time of the last oic_run */
 } oic_stats;

@@ -30,6 +30,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -537,7 +538,19 @@ typedef struct kmer_entry {
   uint64_t occBgn;       /* first occurrence in occ[], insertion order */
   uint32_t occCnt;
   uint32_t empty;        /* screened by the -k skip list */
+  uint32_t firstStr;     /* block string that inserted it first */
+  uint32_t pad;
 } kmer_entry;
+
+/* One partition of the k-mer map: keys are spread over partitions so that the block
+ * can be built by one thread per partition; each partition still sees its k-mers in
+ * the reference's insertion order. */
+typedef struct part_map {
+  uint64_t    mapCap;         /* power of two */
+  int64_t    *map;            /* slot -> entry index or -1 */
+  kmer_entry *ent;
+  uint64_t    nEnt, entCap;
+} part_map;
 
 typedef struct hash_block {
   uint32_t    firstID;        /* Hash_String_Num_Offset */
@@ -547,12 +560,11 @@ typedef struct hash_block {
   uint8_t    *lScreened, *rScreened;
   char       *bases;          /* lowercase, NUL after each read */
   uint64_t    basesLen;
-  uint64_t    mapCap;         /* power of two */
-  int64_t    *map;            /* slot -> entry index or -1 */
-  kmer_entry *ent;
-  uint64_t    nEnt, entCap;
+  int         nParts;
+  part_map   *part;
   uint64_t   *occ;            /* (string << 32) | offset, grouped per entry, insertion order */
   uint64_t    nOcc;
+  uint64_t    nDistinct;
 } hash_block;
 
 static uint64_t mix64(uint64_t x) {
@@ -564,54 +576,68 @@ static uint64_t mix64(uint64_t x) {
   return x;
 }
 
-static int64_t map_find(const hash_block *h, uint64_t key) {
-  uint64_t m = h->mapCap - 1, s = mix64(key) & m;
-  while (h->map[s] >= 0) {
-    if (h->ent[h->map[s]].key == key)
-      return h->map[s];
-    s = (s + 1) & m;
+static int part_of(const hash_block *h, uint64_t key) {
+  return (int)((mix64(key ^ 0x5bd1e9955bd1e995ULL) >> 20) % (uint64_t)h->nParts);
+}
+
+static int64_t pm_find(const part_map *m, uint64_t key) {
+  if (m->mapCap == 0) return -1;
+  uint64_t msk = m->mapCap - 1, s = mix64(key) & msk;
+  while (m->map[s] >= 0) {
+    if (m->ent[m->map[s]].key == key)
+      return m->map[s];
+    s = (s + 1) & msk;
   }
   return -1;
 }
 
-static void map_grow(hash_block *h) {
-  uint64_t nc = h->mapCap ? h->mapCap * 2 : (1u << 16);
+static void pm_grow(part_map *m) {
+  uint64_t nc = m->mapCap ? m->mapCap * 2 : (1u << 16);
   int64_t *nm = (int64_t *)xmalloc(sizeof(int64_t) * nc);
   memset(nm, 0xff, sizeof(int64_t) * nc);
-  for (uint64_t i = 0; i < h->nEnt; i++) {
-    uint64_t s = mix64(h->ent[i].key) & (nc - 1);
+  for (uint64_t i = 0; i < m->nEnt; i++) {
+    uint64_t s = mix64(m->ent[i].key) & (nc - 1);
     while (nm[s] >= 0) s = (s + 1) & (nc - 1);
     nm[s] = (int64_t)i;
   }
-  free(h->map);
-  h->map    = nm;
-  h->mapCap = nc;
+  free(m->map);
+  m->map    = nm;
+  m->mapCap = nc;
 }
 
 /* Find-or-create; returns the entry index and sets *created. */
-static int64_t map_insert(hash_block *h, uint64_t key, int *created) {
-  if ((h->nEnt + 1) * 2 > h->mapCap)
-    map_grow(h);
-  uint64_t m = h->mapCap - 1, s = mix64(key) & m;
-  while (h->map[s] >= 0) {
-    if (h->ent[h->map[s]].key == key) {
+static int64_t pm_insert(part_map *m, uint64_t key, uint32_t str, int *created) {
+  if ((m->nEnt + 1) * 2 > m->mapCap)
+    pm_grow(m);
+  uint64_t msk = m->mapCap - 1, s = mix64(key) & msk;
+  while (m->map[s] >= 0) {
+    if (m->ent[m->map[s]].key == key) {
       *created = 0;
-      return h->map[s];
+      return m->map[s];
     }
-    s = (s + 1) & m;
+    s = (s + 1) & msk;
   }
-  if (h->nEnt == h->entCap) {
-    h->entCap = h->entCap ? h->entCap * 2 : (1u << 16);
-    h->ent    = (kmer_entry *)xrealloc(h->ent, sizeof(kmer_entry) * h->entCap);
+  if (m->nEnt == m->entCap) {
+    m->entCap = m->entCap ? m->entCap * 2 : (1u << 16);
+    m->ent    = (kmer_entry *)xrealloc(m->ent, sizeof(kmer_entry) * m->entCap);
   }
-  kmer_entry *e = &h->ent[h->nEnt];
-  e->key = key;
-  e->occBgn = 0;
-  e->occCnt = 0;
-  e->empty  = 0;
-  h->map[s] = (int64_t)h->nEnt;
-  *created  = 1;
-  return (int64_t)h->nEnt++;
+  kmer_entry *e = &m->ent[m->nEnt];
+  memset(e, 0, sizeof(*e));
+  e->key      = key;
+  e->firstStr = str;
+  m->map[s]   = (int64_t)m->nEnt;
+  *created    = 1;
+  return (int64_t)m->nEnt++;
+}
+
+/* The entry of a k-mer in the loaded block, or NULL.  Entries first created by a read
+ * past the block's end are not part of the block. */
+static kmer_entry *block_find(const hash_block *h, uint64_t key) {
+  part_map *m = &h->part[part_of(h, key)];
+  int64_t   i = pm_find(m, key);
+  if (i < 0) return NULL;
+  kmer_entry *e = &m->ent[i];
+  return (e->firstStr < h->nStrings) ? e : NULL;
 }
 
 static int base_code(char c) {  /* Bit_Equivalent / Char_Is_Bad (overlapInCore.C:500-512) */
@@ -630,43 +656,39 @@ static void free_block(hash_block *h) {
   free(h->lScreened);
   free(h->rScreened);
   free(h->bases);
-  free(h->map);
-  free(h->ent);
+  for (int i = 0; i < h->nParts; i++) {
+    free(h->part[i].map);
+    free(h->part[i].ent);
+  }
+  free(h->part);
   free(h->occ);
   memset(h, 0, sizeof(*h));
 }
 
-typedef struct kmer_iter { uint64_t key; uint32_t bad; } kmer_iter;
-
-/* Insert every ACGT-only k-mer of string `si` (Put_String_In_Hash :329-404). */
-static void put_string(hash_block *h, uint32_t si, uint32_t K, uint64_t *nDistinct, int fill) {
-  const char *s   = h->bases + h->start[si];
-  uint32_t    len = h->length[si];
-  uint64_t    key = 0, mask = (K >= 32) ? ~0ULL : ((1ULL << (2 * K)) - 1);
-  uint32_t    bad = 0;  /* number of non-ACGT among the last K */
-  for (uint32_t i = 0; i < len; i++) {
-    int c = base_code(s[i]);
-    key   = (key >> 2) | ((uint64_t)(c < 0 ? 0 : c) << (2 * (K - 1)));
-    key &= mask;
-    if (c < 0) bad = K;
-    else if (bad > 0) bad--;
-    if (i + 1 < K || bad > 0)
-      continue;
-    uint32_t off = i + 1 - K;
-    int      created;
-    int64_t  ei = map_insert(h, key, &created);
-    if (created) (*nDistinct)++;
-    if (fill)
-      h->occ[h->ent[ei].occBgn + h->ent[ei].occCnt] = ((uint64_t)si << 32) | off;
-    h->ent[ei].occCnt++;
-  }
-}
+/* Walk the ACGT-only k-mers of string si in order (Put_String_In_Hash :329-404),
+ * calling fn for those of partition `part`. */
+#define FOR_KMERS_OF_PART(h, si, K, part, BODY)                                       \
+  do {                                                                                \
+    const char *s_   = (h)->bases + (h)->start[si];                                   \
+    uint32_t    len_ = (h)->length[si];                                               \
+    uint64_t    key  = 0, msk_ = ((K) >= 32) ? ~0ULL : ((1ULL << (2 * (K))) - 1);     \
+    uint32_t    bad_ = 0;                                                             \
+    for (uint32_t i_ = 0; i_ < len_; i_++) {                                          \
+      int c_ = base_code(s_[i_]);                                                     \
+      key    = ((key >> 2) | ((uint64_t)(c_ < 0 ? 0 : c_) << (2 * ((K) - 1)))) & msk_; \
+      if (c_ < 0) bad_ = (K);                                                         \
+      else if (bad_ > 0) bad_--;                                                      \
+      if (i_ + 1 < (K) || bad_ > 0) continue;                                         \
+      if (part_of((h), key) != (part)) continue;                                      \
+      uint32_t off = i_ + 1 - (K);                                                    \
+      BODY                                                                            \
+    }                                                                                 \
+  } while (0)
 
 /* Hash_Mark_Empty (:130-177) with Mark_Screened_Ends_Chain (:96-121). */
 static void mark_empty(hash_block *h, uint64_t key, uint32_t K, int hopeless) {
-  int64_t ei = map_find(h, key);
-  if (ei >= 0) {
-    kmer_entry *e = &h->ent[ei];
+  kmer_entry *e = block_find(h, key);
+  if (e) {
     if (!e->empty) {
       for (uint32_t j = 0; j < e->occCnt; j++) {
         uint64_t o   = h->occ[e->occBgn + j];
@@ -682,9 +704,12 @@ static void mark_empty(hash_block *h, uint64_t key, uint32_t K, int hopeless) {
     return;
   }
   if (hopeless) {  /* Add_Extra_Hash_String (:26-86): an empty entry that only screens */
-    int created;
-    ei = map_insert(h, key, &created);
-    h->ent[ei].empty = 1;
+    int       created;
+    part_map *m  = &h->part[part_of(h, key)];
+    int64_t   ei = pm_insert(m, key, 0, &created);
+    m->ent[ei].firstStr = 0;
+    m->ent[ei].occCnt   = 0;
+    m->ent[ei].empty    = 1;
   }
 }
 
@@ -723,16 +748,22 @@ static int read_skip_file(hash_block *h, const char *path, uint32_t K, int hopel
   return 0;
 }
 
-/* Build_Hash_Index (:414-631).  Returns the last read ID loaded, or 0 on error. */
+/* Build_Hash_Index (:414-631) with one thread per key partition.  The reference loads
+ * reads while the loaded length and the distinct-k-mer count are under their limits
+ * (:504-506); here every read under the length limit is scanned, the distinct k-mers
+ * each read adds are counted, and the block ends where the reference's loop would
+ * stop.  Returns the last read ID loaded, or 0 on error. */
 static uint32_t build_block(hash_block *h, const oic_port_params *p, const oic_seqdb *db, uint32_t bgnID,
-                            uint32_t endID, uint64_t maxDataLen, int *err) {
+                            uint32_t endID, uint64_t maxDataLen, int nThreads, int *err) {
   uint32_t K         = p->kmerLen;
   uint64_t tableSize = (uint64_t)1 << p->hashBits;
   uint64_t entryLim  = (uint64_t)(p->maxHashLoad * (double)tableSize * ENTRIES_PER_BUCKET);
   memset(h, 0, sizeof(*h));
   h->firstID = bgnID;
+  h->nParts  = nThreads < 1 ? 1 : nThreads;
+  h->part    = (part_map *)xcalloc((size_t)h->nParts, sizeof(part_map));
 
-  /* Upper bound on the bases to load (:458-477). */
+  /* Candidate reads under the length limit (:458-477, :504-545). */
   uint64_t maxAlloc = 0;
   for (uint32_t id = bgnID; maxAlloc < maxDataLen && id <= endID; id++) {
     const oic_seqdb_entry *r = &db->index[id - 1];
@@ -746,12 +777,10 @@ static uint32_t build_block(hash_block *h, const oic_port_params *p, const oic_s
   h->lScreened  = (uint8_t *)xcalloc(nIDs, 1);
   h->rScreened  = (uint8_t *)xcalloc(nIDs, 1);
   h->bases      = (char *)xmalloc(maxAlloc + 1);
-
-  /* Pass 1: load reads while under both limits (:504-575), counting distinct k-mers. */
-  uint64_t total = 0, nDistinct = 0;
-  uint32_t cur;
-  for (cur = bgnID; total < maxDataLen && nDistinct < entryLim && cur <= endID; cur++) {
-    uint32_t               si = h->nStrings++;
+  uint64_t total = 0;
+  uint32_t nCand = 0;
+  for (uint32_t cur = bgnID; total < maxDataLen && cur <= endID; cur++, nCand++) {
+    uint32_t               si = nCand;
     const oic_seqdb_entry *r  = &db->index[cur - 1];
     h->start[si]              = -1;
     h->length[si]             = 0;
@@ -770,30 +799,79 @@ static uint32_t build_block(hash_block *h, const oic_port_params *p, const oic_s
     for (uint32_t i = 0; i < r->length; i++)
       h->bases[total++] = (char)tolower((unsigned char)src[i]);
     h->bases[total++] = 0;
-    put_string(h, si, K, &nDistinct, 0);
   }
   h->basesLen = total;
 
-  /* Pass 2: lay occurrences out per entry in insertion order. */
+  /* Insert every candidate's k-mers, counting the new keys each read brings. */
+  const int P       = h->nParts;
+  uint32_t *newKeys = (uint32_t *)xcalloc((size_t)P * nCand + 1, sizeof(uint32_t));
+#pragma omp parallel for num_threads(P) schedule(static, 1)
+  for (int t = 0; t < P; t++) {
+    part_map *m = &h->part[t];
+    for (uint32_t si = 0; si < nCand; si++) {
+      if (h->start[si] < 0) continue;
+      FOR_KMERS_OF_PART(h, si, K, t, {
+        int created;
+        (void)off;
+        pm_insert(m, key, si, &created);
+        if (created) newKeys[(size_t)t * nCand + si]++;
+      });
+    }
+  }
+  uint64_t len = 0, distinct = 0;
+  uint32_t cut;
+  for (cut = 0; cut < nCand; cut++) {
+    if (!(len < maxDataLen && distinct < entryLim)) break;
+    if (h->start[cut] >= 0) len += (uint64_t)h->length[cut] + 1;
+    for (int t = 0; t < P; t++) distinct += newKeys[(size_t)t * nCand + cut];
+  }
+  free(newKeys);
+  h->nStrings  = cut;
+  h->nDistinct = distinct;
+  for (uint32_t si = cut; si < nCand; si++) h->start[si] = -1;
+
+  /* Occurrences of the loaded reads, per entry in insertion order. */
+#pragma omp parallel for num_threads(P) schedule(static, 1)
+  for (int t = 0; t < P; t++) {
+    part_map *m = &h->part[t];
+    for (uint64_t i = 0; i < m->nEnt; i++) m->ent[i].occCnt = 0;
+    for (uint32_t si = 0; si < cut; si++) {
+      if (h->start[si] < 0) continue;
+      FOR_KMERS_OF_PART(h, si, K, t, {
+        (void)off;
+        m->ent[pm_find(m, key)].occCnt++;
+      });
+    }
+  }
   uint64_t acc = 0;
-  for (uint64_t i = 0; i < h->nEnt; i++) {
-    h->ent[i].occBgn = acc;
-    acc += h->ent[i].occCnt;
-    h->ent[i].occCnt = 0;
+  for (int t = 0; t < P; t++) {
+    part_map *m = &h->part[t];
+    for (uint64_t i = 0; i < m->nEnt; i++) {
+      m->ent[i].occBgn = acc;
+      acc += m->ent[i].occCnt;
+      m->ent[i].occCnt = 0;
+    }
   }
   h->nOcc = acc;
   h->occ  = (uint64_t *)xmalloc(sizeof(uint64_t) * (acc ? acc : 1));
-  uint64_t dummy = 0;
-  for (uint32_t si = 0; si < h->nStrings; si++)
-    if (h->start[si] >= 0)
-      put_string(h, si, K, &dummy, 1);
+#pragma omp parallel for num_threads(P) schedule(static, 1)
+  for (int t = 0; t < P; t++) {
+    part_map *m = &h->part[t];
+    for (uint32_t si = 0; si < cut; si++) {
+      if (h->start[si] < 0) continue;
+      FOR_KMERS_OF_PART(h, si, K, t, {
+        kmer_entry *e = &m->ent[pm_find(m, key)];
+        h->occ[e->occBgn + e->occCnt++] = ((uint64_t)si << 32) | off;
+      });
+    }
+  }
 
   if (p->kmerSkipFile && read_skip_file(h, p->kmerSkipFile, K, p->useHopelessCheck)) {
     *err = 1;
     return 0;
   }
   *err = 0;
-  return cur - 1;
+  return bgnID + cut - 1;
 }
 
 /* ------------------------------------------------------------------------------ */
@@ -1226,10 +1304,9 @@ static void find_overlaps(work_area *w, const oic_port_params *p, const hash_blo
     if (i + 1 < (int32_t)K || bad > 0)
       continue;
     int32_t off = i + 1 - (int32_t)K;
-    int64_t ei  = map_find(h, key);
-    if (ei < 0)
+    const kmer_entry *e = block_find(h, key);
+    if (!e)
       continue;
-    const kmer_entry *e = &h->ent[ei];
     if (e->empty) {  /* hi_hits: Find_Overlaps.C:274-276 (offset 0), :310-317 */
       if (off == 0) w->leftScreened = 1;
       else {
@@ -1301,48 +1378,7 @@ static void add_stats(oic_port_stats *d, const oic_port_stats *s) {
   d->candidatePairs += s->candidatePairs;
 }
 
-/* OverlapDriver (overlapInCore.C:161-277) and Process_Overlaps
- * (overlapInCore-Process_Overlaps.C:24-122).                                       */
-int oic_port_run(const oic_port_params *pin, const oic_seqdb *db, oic_port_record **recs, uint64_t *nRecs,
-                 oic_port_stats *stats) {
-  oic_port_params P = *pin;
-  const oic_port_params *p = &P;
-  memset(stats, 0, sizeof(*stats));
-  *recs  = NULL;
-  *nRecs = 0;
-  if (p->kmerLen == 0 || p->kmerLen > 31) {
-    fprintf(stderr, "oic_port: k-mer size must be 1..31\n");
-    return 1;
-  }
-  uint32_t last = db->nReads;
-  if (P.bgnHashID < 1) P.bgnHashID = 1;
-  if (last < P.endHashID) P.endHashID = last;
-  if (P.bgnRefID < 1) P.bgnRefID = 1;
-  if (P.endRefID > last) P.endRefID = last;
-
-  for (uint32_t i = 0; i < db->nReads; i++)
-    if (db->index[i].length > AS_MAX_READLEN) {
-      fprintf(stderr, "oic_port: read %u longer than %u\n", i + 1, AS_MAX_READLEN);
-      return 1;
-    }
-
-  /* A read that passes the length filter but is shorter than k trips an assertion in
-   * Find_Overlaps.C:249 (as a ref read) and reads past its own end in
-   * Build_Hash_Index.C:347-350 (as a hash read); both are rejected here. */
-  for (uint32_t id = 1; id <= last; id++) {
-    const oic_seqdb_entry *r = &db->index[id - 1];
-    if ((int64_t)r->length >= (int64_t)P.minOlapLen && r->length < P.kmerLen) {
-      fprintf(stderr, "oic_port: read %u (length %u) is shorter than the k-mer size %u\n", id, r->length, P.kmerLen);
-      return 1;
-    }
-  }
-
-  uint64_t maxDataLen = P.maxHashDataLen + AS_MAX_READLEN;      /* overlapInCore.C:454 */
-  double   kmerExpect = exp(-1.0 * (double)p->kmerLen * p->maxErate);
-  if (P.minKmers)   /* overlapInCore.C:410-411 */
-    P.minKmers = (int)floor(kmerExpect * (double)((uint64_t)(int64_t)P.minOlapLen - p->kmerLen + 1));
-
-  int nt = (int)(P.numThreads ? P.numThreads : 1);
+static void work_areas_new(work_area **out, int nt, const oic_port_params *p) {
   work_area *wa = (work_area *)xcalloc((size_t)nt, sizeof(work_area));
   for (int t = 0; t < nt; t++) {
     wa[t].al      = oic_port_aligner_new(p->maxErate, p->alignNoise, p->partial);
@@ -1350,6 +1386,116 @@ int oic_port_run(const oic_port_params *pin, const oic_seqdb *db, oic_port_recor
     wa[t].node    = (match_node *)xmalloc(sizeof(match_node) * (size_t)wa[t].nodeCap);
     wa[t].bases   = (char *)xmalloc(AS_MAX_READLEN + 2);
   }
+  *out = wa;
+}
+
+/* Collect the records and counters of the work areas (and reset them). */
+static void work_areas_collect(work_area *wa, int nt, oic_port_record **recs, uint64_t *nRecs, oic_port_stats *stats) {
+  for (int t = 0; t < nt; t++) {
+    wa[t].st.dpCells    = wa[t].al->cells;
+    wa[t].st.slideBases = wa[t].al->slides;
+    wa[t].al->cells = wa[t].al->slides = 0;
+    add_stats(stats, &wa[t].st);
+    memset(&wa[t].st, 0, sizeof(wa[t].st));
+    if (wa[t].nRec) {
+      *recs = (oic_port_record *)xrealloc(*recs, sizeof(oic_port_record) * (size_t)(*nRecs + wa[t].nRec));
+      memcpy(*recs + *nRecs, wa[t].rec, sizeof(oic_port_record) * (size_t)wa[t].nRec);
+      *nRecs += wa[t].nRec;
+      wa[t].nRec = 0;
+    }
+  }
+}
+
+
+static void work_areas_free(work_area *wa, int nt) {
+  for (int t = 0; t < nt; t++) {
+    oic_port_aligner_free(wa[t].al);
+    free(wa[t].node);
+    free(wa[t].pair);
+    free(wa[t].pmap);
+    free(wa[t].rec);
+    free(wa[t].bases);
+  }
+  free(wa);
+}
+
+/* Process_Overlaps (overlapInCore-Process_Overlaps.C:24-122) for ref IDs [lo, hi]:
+ * each ref read forward, then reverse-complemented. */
+static void run_refs(const oic_port_params *p, const oic_seqdb *db, const hash_block *h, work_area *wa, int nt,
+                     int64_t refLo, int64_t refHi, double kmerExpect) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (int64_t fi = refLo; fi <= refHi; fi++) {
+    int t = 0;
+#ifdef _OPENMP
+    t = omp_get_thread_num();
+#endif
+    work_area             *w = &wa[t];
+    const oic_seqdb_entry *r = &db->index[fi - 1];
+    if (r->libID < p->minLibToRef || r->libID > p->maxLibToRef) continue;
+    if ((int64_t)r->length < (int64_t)p->minOlapLen) continue;
+    if (r->length < p->kmerLen) continue;
+    const char *src = db->bases + r->offset;
+    for (uint32_t i = 0; i < r->length; i++)
+      w->bases[i] = (char)tolower((unsigned char)src[i]);
+    w->bases[r->length] = 0;
+    find_overlaps(w, p, h, w->bases, (int32_t)r->length, (uint32_t)fi, 0, kmerExpect);
+    reverse_complement(w->bases, (int32_t)r->length);
+    find_overlaps(w, p, h, w->bases, (int32_t)r->length, (uint32_t)fi, 1, kmerExpect);
+  }
+}
+
+static double wall_seconds(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+/* Checks and derived values shared by the whole-stage run and a session. */
+static int prepare_params(oic_port_params *P, const oic_seqdb *db, double *kmerExpect) {
+  if (P->kmerLen == 0 || P->kmerLen > 31) {
+    fprintf(stderr, "oic_port: k-mer size must be 1..31\n");
+    return 1;
+  }
+  uint32_t last = db->nReads;
+  if (P->bgnHashID < 1) P->bgnHashID = 1;
+  if (last < P->endHashID) P->endHashID = last;
+  if (P->bgnRefID < 1) P->bgnRefID = 1;
+  if (P->endRefID > last) P->endRefID = last;
+  for (uint32_t i = 0; i < db->nReads; i++)
+    if (db->index[i].length > AS_MAX_READLEN) {
+      fprintf(stderr, "oic_port: read %u longer than %u\n", i + 1, AS_MAX_READLEN);
+      return 1;
+    }
+  /* A read that passes the length filter but is shorter than k trips an assertion in
+   * Find_Overlaps.C:249 (as a ref read) and reads past its own end in
+   * Build_Hash_Index.C:347-350 (as a hash read); both are rejected here. */
+  for (uint32_t id = 1; id <= last; id++) {
+    const oic_seqdb_entry *r = &db->index[id - 1];
+    if ((int64_t)r->length >= (int64_t)P->minOlapLen && r->length < P->kmerLen) {
+      fprintf(stderr, "oic_port: read %u (length %u) is shorter than the k-mer size %u\n", id, r->length, P->kmerLen);
+      return 1;
+    }
+  }
+  *kmerExpect = exp(-1.0 * (double)P->kmerLen * P->maxErate);
+  if (P->minKmers)   /* overlapInCore.C:410-411 */
+    P->minKmers = (int)floor(*kmerExpect * (double)((uint64_t)(int64_t)P->minOlapLen - P->kmerLen + 1));
+  if (P->numThreads < 1) P->numThreads = 1;
+  return 0;
+}
+
+/* OverlapDriver (overlapInCore.C:161-277). */
+int oic_port_run(const oic_port_params *pin, const oic_seqdb *db, oic_port_record **recs, uint64_t *nRecs,
+                 oic_port_stats *stats) {
+  oic_port_params P = *pin;
+  double          kmerExpect;
+  memset(stats, 0, sizeof(*stats));
+  *recs  = NULL;
+  *nRecs = 0;
+  if (prepare_params(&P, db, &kmerExpect)) return 1;
+  const oic_port_params *p = &P;
+  int        nt = (int)P.numThreads;
+  work_area *wa;
+  work_areas_new(&wa, nt, p);
 
   /* The ref reads one thread chunk loop visits (Process_Overlaps.C:33; overlapInCore.C:225):
    * every ID in [bgnRef,endRef] except endRef when a chunk would start exactly on it. */
@@ -1360,12 +1506,12 @@ int oic_port_run(const oic_port_params *pin, const oic_seqdb *db, oic_port_recor
       refEnd = P.endRefID - 1;
   }
 
-  int      rc     = 0;
-  uint32_t bgnH   = P.bgnHashID;
-  while (bgnH < P.endHashID && rc == 0) {
+  int      rc   = 0;
+  uint32_t bgnH = P.bgnHashID;
+  while (bgnH < P.endHashID && rc == 0) {   /* overlapInCore.C:204 */
     hash_block h;
     int        err  = 0;
-    uint32_t   endH = build_block(&h, p, db, bgnH, P.endHashID, maxDataLen, &err);
+    uint32_t   endH = build_block(&h, p, db, bgnH, P.endHashID, P.maxHashDataLen + AS_MAX_READLEN, nt, &err);
     if (err) {
       free_block(&h);
       rc = 1;
@@ -1373,48 +1519,69 @@ int oic_port_run(const oic_port_params *pin, const oic_seqdb *db, oic_port_recor
     }
     stats->nHashBlocks++;
     fprintf(stderr, "oic_port: hash block %u-%u (%lu distinct k-mers, %lu occurrences)\n", bgnH, endH,
-            (unsigned long)h.nEnt, (unsigned long)h.nOcc);
-
+            (unsigned long)h.nDistinct, (unsigned long)h.nOcc);
     int64_t refLo = P.bgnRefID, refHi = (P.bgnRefID <= P.endRefID) ? (int64_t)refEnd : (int64_t)P.bgnRefID - 1;
-#pragma omp parallel for schedule(dynamic, 8) num_threads(nt)
-    for (int64_t fi = refLo; fi <= refHi; fi++) {
-      int t = 0;
-#ifdef _OPENMP
-      t = omp_get_thread_num();
-#endif
-      work_area             *w = &wa[t];
-      const oic_seqdb_entry *r = &db->index[fi - 1];
-      if (r->libID < p->minLibToRef || r->libID > p->maxLibToRef) continue;
-      if ((int64_t)r->length < (int64_t)p->minOlapLen) continue;
-      if (r->length < p->kmerLen) continue;
-      const char *src = db->bases + r->offset;
-      for (uint32_t i = 0; i < r->length; i++)
-        w->bases[i] = (char)tolower((unsigned char)src[i]);
-      w->bases[r->length] = 0;
-      find_overlaps(w, p, &h, w->bases, (int32_t)r->length, (uint32_t)fi, 0, kmerExpect);
-      reverse_complement(w->bases, (int32_t)r->length);
-      find_overlaps(w, p, &h, w->bases, (int32_t)r->length, (uint32_t)fi, 1, kmerExpect);
-    }
+    run_refs(p, db, &h, wa, nt, refLo, refHi, kmerExpect);
     free_block(&h);
     bgnH = endH + 1;
   }
-
-  for (int t = 0; t < nt; t++) {
-    wa[t].st.dpCells    = wa[t].al->cells;
-    wa[t].st.slideBases = wa[t].al->slides;
-    add_stats(stats, &wa[t].st);
-    if (wa[t].nRec) {
-      *recs = (oic_port_record *)xrealloc(*recs, sizeof(oic_port_record) * (size_t)(*nRecs + wa[t].nRec));
-      memcpy(*recs + *nRecs, wa[t].rec, sizeof(oic_port_record) * (size_t)wa[t].nRec);
-      *nRecs += wa[t].nRec;
-    }
-    oic_port_aligner_free(wa[t].al);
-    free(wa[t].node);
-    free(wa[t].pair);
-    free(wa[t].pmap);
-    free(wa[t].rec);
-    free(wa[t].bases);
-  }
-  free(wa);
+  uint32_t nb = stats->nHashBlocks;
+  work_areas_collect(wa, nt, recs, nRecs, stats);
+  stats->nHashBlocks = nb;
+  work_areas_free(wa, nt);
   return rc;
+}
+
+struct oic_port_session {
+  oic_port_params  P;
+  const oic_seqdb *db;
+  hash_block       h;
+  work_area       *wa;
+  int              nt;
+  double           kmerExpect;
+  uint32_t         lastLoaded;
+};
+
+oic_port_session *oic_port_session_new(const oic_port_params *pin, const oic_seqdb *db, double *buildSeconds) {
+  oic_port_session *s = (oic_port_session *)xcalloc(1, sizeof(*s));
+  s->P  = *pin;
+  s->db = db;
+  if (prepare_params(&s->P, db, &s->kmerExpect)) {
+    free(s);
+    return NULL;
+  }
+  s->nt     = (int)s->P.numThreads;
+  double t0 = wall_seconds();
+  int    err = 0;
+  s->lastLoaded = build_block(&s->h, &s->P, db, s->P.bgnHashID, s->P.endHashID, s->P.maxHashDataLen + AS_MAX_READLEN,
+                              s->nt, &err);
+  if (buildSeconds) *buildSeconds = wall_seconds() - t0;
+  if (err) {
+    free_block(&s->h);
+    free(s);
+    return NULL;
+  }
+  work_areas_new(&s->wa, s->nt, &s->P);
+  return s;
+}
+
+uint32_t oic_port_session_last_loaded(const oic_port_session *s) { return s->lastLoaded; }
+
+int oic_port_session_refs(oic_port_session *s, uint32_t bgnRef, uint32_t endRef, oic_port_record **recs,
+                          uint64_t *nRecs, oic_port_stats *stats) {
+  memset(stats, 0, sizeof(*stats));
+  *recs  = NULL;
+  *nRecs = 0;
+  if (bgnRef < 1) bgnRef = 1;
+  if (endRef > s->db->nReads) endRef = s->db->nReads;
+  run_refs(&s->P, s->db, &s->h, s->wa, s->nt, bgnRef, endRef, s->kmerExpect);
+  work_areas_collect(s->wa, s->nt, recs, nRecs, stats);
+  return 0;
+}
+
+void oic_port_session_free(oic_port_session *s) {
+  if (!s) return;
+  work_areas_free(s->wa, s->nt);
+  free_block(&s->h);
+  free(s);
 }

@@ -84,6 +84,16 @@ int oic_port_extend(oic_port_aligner *a, const char *S, int32_t sLen, const char
                     int32_t start, int32_t offset, int32_t len, int32_t *out, int32_t *delta,
                     int32_t *deltaLen, uint64_t *cells, uint64_t *slides);
 
+/* A hash block built once (the first block of the -h range) and ref ranges run
+ * against it, for timing the CPU path on a sample of ref reads.  *buildSeconds gets the
+ * wall time of the block build.  numThreads threads are used throughout. */
+typedef struct oic_port_session oic_port_session;
+oic_port_session *oic_port_session_new(const oic_port_params *p, const oic_seqdb *db, double *buildSeconds);
+uint32_t          oic_port_session_last_loaded(const oic_port_session *s);
+int  oic_port_session_refs(oic_port_session *s, uint32_t bgnRef, uint32_t endRef, oic_port_record **recs,
+                           uint64_t *nRecs, oic_port_stats *stats);
+void oic_port_session_free(oic_port_session *s);
+
 #ifdef __cplusplus
 }
 #endif
