@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 overlapInCore path (one JSON line on stdout, rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2] [--scale 1.0]
+
+A step is one whole overlapInCore job on the workload's read set: the hash block of
+all reads, then every read (both strands) against it -- seed lookup, per-pair match
+lists, and the banded edit-distance extensions that emit the overlap records.
+
+  value  overlaps/s with the reads already resident in HBM (CUDA-event time of the
+         job on the library's stream);
+  e2e    the same through the C ABI with host buffers: every step uploads the reads
+         from pinned host memory, runs the job and copies the records back (wall clock).
+
+--impl reference times the CPU restatement of the reference (oracle/oic_port.c, the
+reference's algorithm step for step; canu's own sources cannot be built on the GPU
+host) on all host cores: the hash block is built once and timed, each step runs a
+sample of ref reads against it, and a step's rate charges the sample its share of the
+block build -- the full job's rate, extrapolated from the sample.
+
+Multi-GPU (torchrun): every rank runs an independent replica on its own GPU (the
+stage shards into independent jobs; there is no data exchange), value = all ranks'
+overlaps / the slowest rank's time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD_TEXT = {
+    "c2": ("c2: 50 Mbp genome with 200 x 6 kb repeat copies (1% divergence) and 2% 171 bp tandem arrays; 30x "
+           "HiFi-like reads (normal 15+-3 kb), 0.5% errors, 50% reverse-complemented; k=22, --minlength 1000, "
+           "--maxerate 0.01, --hashbits 25, --hashdatalen 1.6e9; frequent-k-mer skip list (genome multiplicity "
+           "> 10)"),
+    "c1": ("c1: 5 Mbp iid genome, 20x lognormal reads (8+-3 kb, 1-30 kb), 2% errors 1:1:1; k=22, --minlength 500, "
+           "--maxerate 0.06, --hashbits 23"),
+    "c3": ("c3: 20 Mbp iid genome, 25x Pareto reads (alpha 1.5, 0.5-100 kb), 5% errors 1:2:2; --maxerate 0.12"),
+}
+
+# Nominal INT32 lanes per SM (Blackwell: 128 unified FP32/INT32 lanes).
+INT_LANES_PER_SM = 128
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.proc, self.lines = gpu, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value, ws):
+    """max over ranks (and a barrier)."""
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------------
+# CPU path (the oracle, test infrastructure)
+
+class PortParams(ctypes.Structure):
+    _fields_ = [("maxErate", ctypes.c_double), ("alignNoise", ctypes.c_double), ("partial", ctypes.c_int),
+                ("bgnHashID", ctypes.c_uint32), ("endHashID", ctypes.c_uint32),
+                ("minLibToHash", ctypes.c_uint32), ("maxLibToHash", ctypes.c_uint32),
+                ("bgnRefID", ctypes.c_uint32), ("endRefID", ctypes.c_uint32),
+                ("minLibToRef", ctypes.c_uint32), ("maxLibToRef", ctypes.c_uint32),
+                ("kmerLen", ctypes.c_uint32), ("kmerSkipFile", ctypes.c_char_p), ("minKmers", ctypes.c_int),
+                ("uniqueOlapPerPair", ctypes.c_int), ("hashBits", ctypes.c_uint32),
+                ("maxHashDataLen", ctypes.c_uint64), ("maxHashLoad", ctypes.c_double),
+                ("numThreads", ctypes.c_uint32), ("minOlapLen", ctypes.c_int32), ("useHopelessCheck", ctypes.c_int)]
+
+
+class PortStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "kmerHitsWithoutOlap", "kmerHitsWithOlap", "kmerHitsSkipped", "multiOverlap", "totalOverlaps",
+        "containedOverlaps", "dovetailOverlaps", "badShortWindow", "badLongWindow", "dpCells", "slideBases",
+        "extensions", "seeds", "candidatePairs")] + [("nHashBlocks", ctypes.c_uint32)]
+
+
+class CpuPath:
+    """The oracle on all host cores: block built once, ref samples timed against it."""
+
+    def __init__(self, wl, db, skip, threads):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "liboic_port.so"))
+        lib.oic_port_seqdb_load.restype = ctypes.c_void_p
+        lib.oic_port_seqdb_load.argtypes = [ctypes.c_char_p]
+        lib.oic_port_session_new.restype = ctypes.c_void_p
+        lib.oic_port_session_new.argtypes = [ctypes.POINTER(PortParams), ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_double)]
+        lib.oic_port_session_refs.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                              ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(PortStats)]
+        lib.oic_port_records_free.argtypes = [ctypes.c_void_p]
+        lib.oic_port_session_free.argtypes = [ctypes.c_void_p]
+        lib.oic_port_seqdb_free.argtypes = [ctypes.c_void_p]
+        lib.oic_port_default_params.argtypes = [ctypes.POINTER(PortParams)]
+        self.lib = lib
+        from canu_gb300 import workloads
+        g = workloads.WORKLOADS[wl]["params"]
+        p = PortParams()
+        lib.oic_port_default_params(ctypes.byref(p))
+        p.maxErate = float(np.float32(g["maxErate"]))
+        p.kmerLen = g["kmerLen"]
+        p.hashBits = g["hashBits"]
+        p.maxHashDataLen = g["maxHashDataLen"]
+        p.maxHashLoad = g.get("maxHashLoad", 0.6)
+        p.minOlapLen = g["minOlapLen"]
+        p.numThreads = threads
+        if p.maxErate > 0.06:
+            p.useHopelessCheck = 0
+        self._skip = skip.encode() if skip else None
+        p.kmerSkipFile = self._skip
+        self.db = lib.oic_port_seqdb_load(db.encode())
+        from canu_gb300 import read_seqdb
+        self.nReads = len(read_seqdb(db)[1])
+        bs = ctypes.c_double()
+        self.sess = lib.oic_port_session_new(ctypes.byref(p), self.db, ctypes.byref(bs))
+        if not self.sess:
+            raise RuntimeError("oracle session failed")
+        self.build_s = bs.value
+
+    def sample(self, bgn, end):
+        recs = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        st = PortStats()
+        t0 = time.perf_counter()
+        self.lib.oic_port_session_refs(self.sess, bgn, end, ctypes.byref(recs), ctypes.byref(n), ctypes.byref(st))
+        dt = time.perf_counter() - t0
+        self.lib.oic_port_records_free(recs)
+        return dt, st
+
+    def close(self):
+        self.lib.oic_port_session_free(self.sess)
+        self.lib.oic_port_seqdb_free(self.db)
+
+    def rate(self, dt, nref, overlaps):
+        """Overlaps/s of the full job: the sample's time plus its share of the block build."""
+        return overlaps / (dt + self.build_s * nref / self.nReads)
+
+
+def cpu_sample(cpu, start, target_s=15.0, chunk=64):
+    """Run ref chunks from `start` until about target_s seconds of CPU work."""
+    dt_tot, ov, nref, cells = 0.0, 0, 0, 0
+    b = start
+    while dt_tot < target_s and b <= cpu.nReads:
+        e = min(cpu.nReads, b + chunk - 1)
+        dt, st = cpu.sample(b, e)
+        dt_tot += dt
+        ov += st.totalOverlaps
+        cells += st.dpCells
+        nref += e - b + 1
+        b = e + 1
+    return dt_tot, ov, nref, cells, b
+
+
+# ----------------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--data-dir", default=os.environ.get("OIC_BENCH_DATA", "/tmp/oic_bench"))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    ws, rank, local = dist()
+    cores = os.cpu_count() or 1
+
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    import canu_gb300 as oic
+    from canu_gb300 import workloads
+
+    if ws > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        td.barrier()
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        db, skip = workloads.generate(a.workload, a.data_dir, a.scale)
+        cpu = CpuPath(a.workload, db, skip, cores)
+        vals, ovs, samples = [], 0, []
+        start = 1
+        for i in range(a.warmup + a.steps):
+            per = max(2.0, a.cpu_seconds / max(1, a.steps))
+            dt, ov, nref, cells, start = cpu_sample(cpu, start if start <= cpu.nReads else 1, per)
+            if i >= a.warmup:
+                vals.append(cpu.rate(dt, nref, ov))
+                samples.append((dt, nref, ov))
+        cpu.close()
+        v = statistics.mean(vals)
+        nrefs = sum(s[1] for s in samples)
+        line = {"impl": "reference", "metric": "overlaps_per_sec", "value": v, "unit": "overlaps/s", "n_gpus": 0,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * statistics.mean(s[0] for s in samples),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+                "data": "synthetic", "config": {"workload": WORKLOAD_TEXT.get(a.workload, a.workload),
+                                                "scale": a.scale, "reads": cpu.nReads},
+                "cpu_baseline": {"value": v, "unit": "overlaps/s", "cores": cores, "kind": "port",
+                                 "sample": f"{nrefs} ref reads (both strands) against the full hash block; block "
+                                           f"build {cpu.build_s:.1f} s charged pro rata; full-job rate "
+                                           f"extrapolated"},
+                "e2e": {"value": v, "unit": "overlaps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    # ------------------------------------------------------------------ our arm
+    if rank == 0:
+        db, skip = workloads.generate(a.workload, a.data_dir, a.scale)
+    if ws > 1:
+        td.barrier()
+    db, skip = workloads.generate(a.workload, a.data_dir, a.scale)
+    lib_, ln, off, bases = oic.read_seqdb(db)
+    nReads = len(ln)
+    try:
+        import torch
+        pinned = torch.empty(bases.size, dtype=torch.uint8, pin_memory=True)
+        pinned.numpy()[:] = bases
+        host_bases = pinned.numpy()
+        pinned_ok = True
+    except Exception:
+        host_bases = np.ascontiguousarray(bases)
+        pinned_ok = False
+
+    p = workloads.params(a.workload)
+    ov = oic.Overlapper(p, device=local if ws > 1 else 0)
+    if skip:
+        ov.set_skip_kmers(workloads.read_skip(skip))
+    ov.set_reads(lib_, ln, off, host_bases)
+
+    peaks, peak_kind = measured_peaks()
+    clocks = Clocks(local)
+    res = []
+    for i in range(a.warmup + a.steps):
+        if i == a.warmup:
+            barrier_max(0.0, ws)
+            clocks.start()
+        t0 = time.perf_counter()
+        ov.clear()
+        ov.set_reads(lib_, ln, off, host_bases)        # H2D of the step's input (pinned)
+        ov.run()
+        rec = ov.overlaps()                            # D2H of the step's result
+        t1 = time.perf_counter()
+        st = ov.stats()
+        if i >= a.warmup:
+            res.append((st, t1 - t0, len(rec)))
+    clk = clocks.stop()
+    ov.close()
+
+    ms_dev = statistics.mean(r[0]["msTotal"] for r in res)
+    s_e2e = statistics.mean(r[1] for r in res)
+    st0 = res[0][0]
+    n_ov = st0["totalOverlaps"]
+    ms_dev_max = barrier_max(ms_dev, ws)
+    s_e2e_max = barrier_max(s_e2e, ws)
+    value = ws * n_ov / (ms_dev_max / 1000.0)
+    e2e = ws * n_ov / s_e2e_max
+
+    # Roofline of the dominant kernel, the pair DP (align_kernel).
+    ms_align = statistics.mean(r[0]["msAlign"] for r in res)
+    pairs, nodes, cells, slides = st0["candidatePairs"], st0["nodes"], st0["dpCells"], st0["slideBases"]
+    mean_len = float(ln.mean())
+    alg_bytes = pairs * (32 + 72 + 4 + 2 * mean_len / 4) + nodes * 16
+    achieved = alg_bytes / (ms_align / 1000.0) / 1e9
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
+    int_ops = 6 * cells + slides / 16.0
+    line = {
+        "metric": "overlaps_per_sec", "value": value, "unit": "overlaps/s", "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_dev_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_TEXT.get(a.workload, a.workload), "scale": a.scale, "reads": nReads,
+                   "bases": int(bases.size), "overlaps_per_step": n_ov, "parallelism": f"replicas{ws}",
+                   "l2": "inputs (2-bit reads, hash table, seed lists) larger than L2"},
+        "dp_cells_per_sec": ws * cells / (ms_dev_max / 1000.0),
+        "work": {"seeds": st0["seeds"], "candidate_pairs": pairs, "match_nodes": nodes, "extensions": st0["extensions"],
+                 "dp_cells": cells, "dp_rows": st0.get("dpRows"), "slide_bases": slides,
+                 "ms_hash": statistics.mean(r[0]["msHash"] for r in res),
+                 "ms_seed": statistics.mean(r[0]["msSeed"] for r in res), "ms_align": ms_align},
+        "e2e": {"value": e2e, "unit": "overlaps/s", "h2d_bytes_per_step": int(host_bases.nbytes + ln.nbytes * 3 + off.nbytes),
+                "d2h_bytes_per_step": int(n_ov * 24), "pinned": pinned_ok, "timing": "wall clock"},
+        "roofline": {"bound": "hbm", "kernel": "align_kernel", "achieved": achieved,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                     "traffic": None, "peak_kind": peak_kind,
+                     "int_ops": {"achieved_tops": int_ops / (ms_align / 1000.0) / 1e12, "peak_tops": int_peak,
+                                 "frac": int_ops / (ms_align / 1000.0) / 1e12 / int_peak,
+                                 "basis": "6 INT ops per DP cell + 1/16 per slide base; peak = 152 SMs x 128 "
+                                          "INT32 lanes x median SM clock"}},
+        "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in res)),
+        "clocks": clk,
+    }
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        cpu = CpuPath(a.workload, db, skip, cores)
+        dt, ovs, nref, ccells, _ = cpu_sample(cpu, 1, a.cpu_seconds)
+        cpu.close()
+        line["cpu_baseline"] = {"value": cpu.rate(dt, nref, ovs), "unit": "overlaps/s", "cores": cores,
+                                "kind": "port",
+                                "sample": f"{nref} ref reads (both strands) against the full hash block "
+                                          f"({dt:.1f} s); block build {cpu.build_s:.1f} s charged pro rata; "
+                                          f"full-job rate extrapolated; {ccells} DP cells"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        td.barrier()
+        td.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

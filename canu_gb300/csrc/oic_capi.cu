@@ -607,6 +607,10 @@ int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const ui
   ctx->wordOff[nReads] = w;
   const uint64_t nWords = w + 2;
 
+  cudaEvent_t r0, r1;
+  cudaEventCreate(&r0);
+  cudaEventCreate(&r1);
+  cudaEventRecord(r0, ctx->st);
   CK(ctx->dFwd.ensure(nWords * 8));
   CK(ctx->dRc.ensure(nWords * 8));
   CK(ctx->dNfwd.ensure(nWords * 8));
@@ -639,6 +643,13 @@ int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const ui
     if (rc) return rc;
     if (err & kErrBadBase) return fail(ctx, OIC_ERR_INPUT, "a read holds a character other than A, C, G, T or N");
   }
+  cudaEventRecord(r1, ctx->st);
+  cudaEventSynchronize(r1);
+  float msR = 0;
+  cudaEventElapsedTime(&msR, r0, r1);
+  cudaEventDestroy(r0);
+  cudaEventDestroy(r1);
+  ctx->stats.msReads = msR;
   ReadsDev &R = ctx->R;
   R.fwd     = ctx->dFwd.as<u64>();
   R.rc      = ctx->dRc.as<u64>();
@@ -927,6 +938,7 @@ int oic_run(oic_ctx *ctx) {
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, ctx->st);
+  const unsigned long long launches0 = g_launches;
   int rc = OIC_OK;
   uint32_t bgnH = G.bgnHashID;
   while (bgnH < G.endHashID) {   // overlapInCore.C:204
@@ -940,6 +952,7 @@ int oic_run(oic_ctx *ctx) {
   float ms = 0;
   cudaEventElapsedTime(&ms, t0, t1);
   ctx->stats.msTotal += ms;
+  ctx->stats.kernelLaunches += g_launches - launches0;
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   return rc;
@@ -962,7 +975,9 @@ int oic_fetch_overlaps(oic_ctx *ctx, uint32_t *words, uint64_t maxRecords, uint6
 int oic_clear_overlaps(oic_ctx *ctx) {
   if (!ctx) return OIC_ERR_ARG;
   ctx->out.clear();
+  const double msReads = ctx->stats.msReads;
   ctx->stats = oic_stats{};
+  ctx->stats.msReads = msReads;
   return OIC_OK;
 }
 

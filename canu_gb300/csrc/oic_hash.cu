@@ -9,6 +9,7 @@
 // reference's chain order).  The distinct-k-mer load limit that ends a block
 // (:445, :504-506) is found from the first occurrence of every key.
 #include "oic_kernels.cuh"
+#include "oic_prims.cuh"
 
 namespace oic {
 
@@ -226,6 +227,7 @@ void launch_pack_reads(const char *ascii, const u64 *srcOff, const u32 *len, con
   if (nReads == 0) return;
   unsigned g = nReads < 65535u * 4 ? nReads : 65535u * 4;
   pack_reads_kernel<<<g, 128, 0, st>>>(ascii, srcOff, len, wordOff, nReads, fwd, rc, nfwd, nrc, hasN, err);
+  g_launches++;
 }
 
 void launch_kmer_emit(ReadsDev R, const u32 *strRead, const u32 *strKmers, const u64 *flatStart, u32 nStr, int K,
@@ -233,34 +235,41 @@ void launch_kmer_emit(ReadsDev R, const u32 *strRead, const u32 *strKmers, const
   if (nStr == 0) return;
   unsigned g = nStr < 65535u * 4 ? nStr : 65535u * 4;
   kmer_emit_kernel<<<g, 256, 0, st>>>(R, strRead, strKmers, flatStart, nStr, K, keys, vals);
+  g_launches++;
 }
 
 void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, int K, u32 *newKeys,
                       cudaStream_t st) {
   if (n == 0) return;
   first_occ_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, vals, n, flatStart, nStr, K, newKeys);
+  g_launches++;
 }
 
 void launch_keep_flags(const u64 *keys, const u32 *vals, u64 n, int K, u32 flatLimit, u32 *flags, cudaStream_t st) {
   if (n == 0) return;
   keep_flags_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, vals, n, K, flatLimit, flags);
+  g_launches++;
 }
 
 void launch_compact_kv(const u64 *keys, const u32 *vals, const u32 *flags, const u32 *pos, u64 n, u64 *keysOut,
                        u32 *valsOut, cudaStream_t st) {
   if (n == 0) return;
   compact_kv_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, vals, flags, pos, n, keysOut, valsOut);
+  g_launches++;
 }
 
 void launch_table_build(const u64 *keys, u64 n, u64 *tKeys, u64 *tVals, u64 mask, u32 *err, cudaStream_t st) {
   if (n == 0) return;
   table_starts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKeys, tVals, mask, err);
+  g_launches++;
   table_counts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKeys, tVals, mask);
+  g_launches++;
 }
 
 void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, u64 *occ, cudaStream_t st) {
   if (n == 0) return;
   occ_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(vals, n, flatStart, nStr, occ);
+  g_launches++;
 }
 
 void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeysMut, u64 *tValsMut, unsigned char *lscr,
@@ -268,6 +277,7 @@ void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeysMut,
   if (nSkip == 0) return;
   skip_mark_kernel<<<grid_for(nSkip, 128), 128, 0, st>>>(skipKeys, nSkip, T, tKeysMut, tValsMut, lscr, rscr, K,
                                                          hopeless, err);
+  g_launches++;
 }
 
 }  // namespace oic

@@ -14,6 +14,7 @@
 // capacity of this configuration are queued for a wider configuration and leave no
 // output or counts behind.
 #include "oic_kernels.cuh"
+#include "oic_prims.cuh"
 
 namespace oic {
 
@@ -556,10 +557,12 @@ void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml
     auto k = align_kernel<512, kAlignWarpsSmall>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
+  g_launches++;
   } else {
     auto k = align_kernel<8192, kAlignWarpsLarge>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
+  g_launches++;
   }
 }
 
@@ -575,10 +578,12 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
     auto k = extend_batch_kernel<512, kAlignWarpsSmall>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
+  g_launches++;
   } else {
     auto k = extend_batch_kernel<8192, kAlignWarpsLarge>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
+  g_launches++;
   }
 }
 
@@ -587,6 +592,7 @@ void launch_work_keys(const PairRec *pairs, u32 n, unsigned long long *keys, u32
   unsigned g = (n + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
   work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, keys, vals);
+  g_launches++;
 }
 
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st) {
@@ -594,6 +600,7 @@ void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 
   unsigned g = (nPairs + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
   compact_records_kernel<<<g, 256, 0, st>>>(rec, cnt, pos, nPairs, dst);
+  g_launches++;
 }
 
 }  // namespace oic

@@ -8,6 +8,8 @@
 
 namespace oic {
 
+unsigned long long g_launches = 0;
+
 namespace {
 
 constexpr int kScanThreads = 256;
@@ -99,15 +101,18 @@ cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *to
   uint64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb == 1) {
     scan_tile_kernel<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr, total);
+    g_launches++;
     return cudaGetLastError();
   }
   uint32_t *sums = (uint32_t *)scratch;
   size_t    here = ((nb * sizeof(uint32_t)) + 255) & ~(size_t)255;
   scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(in, n, sums);
+    g_launches++;
   cudaError_t e = scan_u32(sums, sums, nb, total, (char *)scratch + here, st);
   if (e != cudaSuccess) return e;
   // The recursive call scans `sums` in place into block offsets.
   scan_tile_kernel<<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, sums, nullptr);
+    g_launches++;
   return cudaGetLastError();
 }
 
@@ -221,10 +226,12 @@ cudaError_t radix_sort_u64_u32(unsigned long long *keys, uint32_t *vals, unsigne
   int       passes = 0;
   for (int shift = 0; shift < bits; shift += 8, passes++) {
     radix_upsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, n, shift, hist, (uint32_t)nTiles);
+    g_launches++;
     cudaError_t e = scan_u32(hist, hist, nh, nullptr, scanSc, st);
     if (e != cudaSuccess) return e;
     radix_downsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, vs, kd, vd, n, shift, hist,
                                                                        (uint32_t)nTiles);
+    g_launches++;
     unsigned long long *tk = ks; ks = kd; kd = tk;
     uint32_t *tv = vs; vs = vd; vd = tv;
   }

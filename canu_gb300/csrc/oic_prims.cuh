@@ -8,6 +8,9 @@
 
 namespace oic {
 
+// Kernels launched by this library since load (for launch accounting).
+extern unsigned long long g_launches;
+
 // Scratch bytes oic_scan_u32 needs for n elements.
 size_t scan_u32_scratch(uint64_t n);
 // out[i] = sum(in[0..i)) for i < n, and *total (device pointer, may be null) = sum(in).

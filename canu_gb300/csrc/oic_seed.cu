@@ -14,6 +14,7 @@
 // group's seeds in lane order.  Different partners advance in parallel; one partner's
 // seeds stay in order.  The pair table and node pool live in the warp's HBM scratch.
 #include "oic_kernels.cuh"
+#include "oic_prims.cuh"
 
 namespace oic {
 
@@ -317,6 +318,7 @@ void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, u32 n
   if (nSeg == 0) return;
   int blocks = (nWarps + kSeedWarps - 1) / kSeedWarps;
   seed_kernel<<<blocks, kSeedThreads, 0, st>>>(R, T, P, segReads, nSeg, segCounter, sc, cap, out);
+  g_launches++;
 }
 
 }  // namespace oic

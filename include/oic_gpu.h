@@ -64,7 +64,9 @@ typedef struct oic_stats {
   uint64_t badShortWindow, badLongWindow;
   uint64_t dpCells, slideBases, extensions, seeds, candidatePairs, nodes, dpRows;
   uint32_t nHashBlocks, reserved;
-  double   msHash, msSeed, msAlign, msTotal;       /* device time of the last oic_run */
+  double   msHash, msSeed, msAlign, msTotal;       /* device time (CUDA events) of oic_run work */
+  double   msReads;                                /* device time of the last oic_set_reads */
+  uint64_t kernelLaunches;                         /* kernels launched by oic_run and its parts */
 } oic_stats;
 
 typedef struct oic_ctx oic_ctx;

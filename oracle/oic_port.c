@@ -1585,3 +1585,20 @@ void oic_port_session_free(oic_port_session *s) {
   free_block(&s->h);
   free(s);
 }
+
+oic_seqdb *oic_port_seqdb_load(const char *path) {
+  oic_seqdb *db = (oic_seqdb *)xcalloc(1, sizeof(oic_seqdb));
+  if (oic_seqdb_load(path, db)) {
+    free(db);
+    return NULL;
+  }
+  return db;
+}
+
+void oic_port_seqdb_free(oic_seqdb *db) {
+  if (!db) return;
+  oic_seqdb_free(db);
+  free(db);
+}
+
+void oic_port_records_free(oic_port_record *r) { free(r); }

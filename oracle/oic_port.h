@@ -94,6 +94,11 @@ int  oic_port_session_refs(oic_port_session *s, uint32_t bgnRef, uint32_t endRef
                            uint64_t *nRecs, oic_port_stats *stats);
 void oic_port_session_free(oic_port_session *s);
 
+/* Loading and freeing helpers for callers outside C (ctypes). */
+oic_seqdb *oic_port_seqdb_load(const char *path);
+void       oic_port_seqdb_free(oic_seqdb *db);
+void       oic_port_records_free(oic_port_record *r);
+
 #ifdef __cplusplus
 }
 #endif
