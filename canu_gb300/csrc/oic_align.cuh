@@ -43,6 +43,18 @@ struct WarpDP {
   int                leftLen, rightLen;
 };
 
+// The scratch of global warp gw inside the base allocations of a configuration.
+static __device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &base, const AlignCaps &cap, u64 gw) {
+  WarpScratch s;
+  s.arena  = base.arena + gw * (u64)cap.arenaCap;
+  s.rowHdr = base.rowHdr + gw * (u64)cap.rowCap;
+  s.deltaL = base.deltaL + gw * (u64)(cap.rowCap + 8);
+  s.deltaR = base.deltaR + gw * (u64)(cap.rowCap + 8);
+  s.stack  = base.stack + gw * (u64)(cap.rowCap + 8);
+  s.alive  = base.alive + gw * (u64)cap.nodeCap;
+  return s;
+}
+
 // Row-0 exact slide shared by the warp: each lane tests one 32-base window per step.
 template <int STEP>
 __device__ __forceinline__ int warp_slide0(const SeqView &A, i64 a0, const SeqView &T, i64 t0, int m,

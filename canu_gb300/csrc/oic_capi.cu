@@ -135,7 +135,7 @@ struct oic_ctx {
   TableDev T{};
 
   // seeds
-  DevBuf dSegReads, dPairs, dNodes, dSegOvf;
+  DevBuf dSegReads, dPairs, dNodes, dSegOvf, dSegList;
   DevBuf dSeedSlotK, dSeedSlotV, dSeedPairs, dSeedNodes;        // normal configuration
   DevBuf dSeedSlotK2, dSeedSlotV2, dSeedPairs2, dSeedNodes2;    // wide configuration
   uint32_t pairCap = 0, nodeCap = 0;
@@ -321,48 +321,31 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   SeedScratch ss;
   int rc = ensure_seed_scratch(ctx, sn, false, ss);
   if (rc) return rc;
-  launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), nSeg, ctr32(ctx) + cSegCounter, ss, sn.caps,
-              sn.warps, so, ctx->st);
+  launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), nullptr, nSeg, ctr32(ctx) + cSegCounter, ss,
+              sn.caps, sn.warps, so, ctx->st);
   uint32_t h[16];
   CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
   if ((rc = sync_check(ctx, "seed kernel"))) return rc;
   if (h[cErr] & (kErrOutNodes | kErrOutPairs)) return kRetrySmaller;
   if (h[cSegOvf] > 0) {
-    // Segments whose pair table or node pool overflowed: rerun them wide.
+    // Segments whose pair table or node pool overflowed run again in the wide
+    // configuration; their ids are the work list of that pass.
     const uint32_t nOvf = h[cSegOvf];
-    std::vector<uint32_t> segs(nOvf), reads(nOvf);
-    CK(cudaMemcpyAsync(segs.data(), ctx->dSegOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
-    // A wide pass takes whole segments: encode each as its own (read, strand) pair.
-    std::vector<uint32_t> segReads2(nOvf);
-    for (uint32_t i = 0; i < nOvf; i++) segReads2[i] = refs[segs[i] >> 1];
-    DevBuf segBuf;
-    // Run strand by strand so that segment ids stay (read << 1 | strand).
+    if (verbose()) fprintf(stderr, "oic: %u ref strands rerun in the wide seed configuration\n", nOvf);
+    CK(ctx->dSegList.ensure((size_t)nOvf * sizeof(uint32_t)));
+    CK(cudaMemcpyAsync(ctx->dSegList.p, ctx->dSegOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cSegCounter, 0, sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cSegOvf, 0, sizeof(uint32_t), ctx->st));
     SeedConfig sw = seed_wide(ctx);
     SeedScratch ssw;
     if ((rc = ensure_seed_scratch(ctx, sw, true, ssw))) return rc;
-    for (uint32_t i = 0; i < nOvf; i++) {
-      // one segment at a time through a 2-entry segment list: [read] with the strand picked by the id
-      uint32_t strand = segs[i] & 1;
-      uint32_t rd     = segReads2[i];
-      CK(segBuf.ensure(sizeof(uint32_t)));
-      CK(cudaMemcpyAsync(segBuf.p, &rd, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
-      CK(cudaMemsetAsync(ctr32(ctx) + cSegCounter, 0, sizeof(uint32_t), ctx->st));
-      // nSeg = strand + 1 and counter pre-set to `strand` selects exactly segment `strand`.
-      uint32_t start = strand;
-      CK(cudaMemcpyAsync(ctr32(ctx) + cSegCounter, &start, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
-      CK(cudaMemsetAsync(ctr32(ctx) + cSegOvf, 0, sizeof(uint32_t), ctx->st));
-      launch_seed(ctx->R, ctx->T, ctx->dp, segBuf.as<uint32_t>(), strand + 1, ctr32(ctx) + cSegCounter, ssw, sw.caps,
-                  sw.warps, so, ctx->st);
-      CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-      if ((rc = sync_check(ctx, "seed kernel (wide)"))) { segBuf.release(); return rc; }
-      if (h[cErr] & (kErrOutNodes | kErrOutPairs)) { segBuf.release(); return kRetrySmaller; }
-      if (h[cSegOvf] > 0) {
-        segBuf.release();
-        return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
-      }
-    }
-    segBuf.release();
+    launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), ctx->dSegList.as<uint32_t>(), nOvf,
+                ctr32(ctx) + cSegCounter, ssw, sw.caps, sw.warps, so, ctx->st);
+    CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = sync_check(ctx, "seed kernel (wide)"))) return rc;
+    if (h[cErr] & (kErrOutNodes | kErrOutPairs)) return kRetrySmaller;
+    if (h[cSegOvf] > 0)
+      return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
   }
   CK(cudaEventRecord(evSeed1, ctx->st));
   const uint32_t nPairs = h[cPairCount];
@@ -572,7 +555,7 @@ void oic_destroy(oic_ctx *ctx) {
                     &ctx->dDL,       &ctx->dDR,         &ctx->dStack,      &ctx->dAlive,     &ctx->dArena2,
                     &ctx->dRowHdr2,  &ctx->dDL2,       &ctx->dDR2,
                     &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr,
-                    &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch};
+                    &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch, &ctx->dSegList};
   for (DevBuf *b : bufs) b->release();
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
@@ -867,12 +850,12 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
   size_t freeB = 0, totalB = 0;
   cudaMemGetInfo(&freeB, &totalB);
   if (ctx->pairCap == 0) {
-    ctx->pairCap = 8u << 20;
-    ctx->nodeCap = 256u << 20;
-    if (freeB < ((size_t)48 << 30)) {
-      ctx->pairCap = 2u << 20;
-      ctx->nodeCap = 32u << 20;
-    }
+    // Per pair: the record (32 B), three output slots (72 B) and the work-list,
+    // count and position words; per node 16 B.  Take about a fifth of the free memory.
+    const size_t budget = freeB / 5;
+    size_t pc = std::min<size_t>(32u << 20, budget / 3 / 160), nc = std::min<size_t>(1u << 29, budget * 2 / 3 / 16);
+    ctx->pairCap = (uint32_t)std::max<size_t>(pc, 1u << 16);
+    ctx->nodeCap = (uint32_t)std::max<size_t>(nc, 1u << 20);
     CK(ctx->dPairs.ensure((size_t)ctx->pairCap * sizeof(PairRec)));
     CK(ctx->dNodes.ensure((size_t)ctx->nodeCap * sizeof(int4)));
   }
@@ -899,6 +882,13 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
     }
     if (rc) break;
     pos += nb;
+    // Size the next batch from the pair and node density seen so far (25% headroom).
+    const double pr = (double)(ctx->stats.candidatePairs - saved.candidatePairs) / nb;
+    const double nr = (double)(ctx->stats.nodes - saved.nodes) / nb;
+    double lim = (double)refs.size();
+    if (pr > 0) lim = std::min(lim, 0.8 * ctx->pairCap / pr);
+    if (nr > 0) lim = std::min(lim, 0.8 * ctx->nodeCap / nr);
+    batch = (uint32_t)std::max(1.0, std::min(lim, (double)refs.size()));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

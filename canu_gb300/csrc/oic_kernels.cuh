@@ -77,8 +77,9 @@ struct SeedOut {
   u32     *err;
 };
 
-void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, u32 nSeg, u32 *segCounter, SeedScratch sc,
-                 SeedCaps cap, int nWarps, SeedOut out, cudaStream_t st);
+// Segment k is (ref index << 1 | strand) = segList[k], or k when segList is null.
+void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, const u32 *segList, u32 nSeg,
+                 u32 *segCounter, SeedScratch sc, SeedCaps cap, int nWarps, SeedOut out, cudaStream_t st);
 
 // ---------------- pairs / DP ----------------
 struct AlignOut {

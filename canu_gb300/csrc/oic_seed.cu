@@ -85,8 +85,8 @@ __device__ __forceinline__ bool add_match(int4 *nodes, SeedSmem &sm, int nodeCap
 }
 
 __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev T, DevParams P, const u32 *segReads,
-                                                            u32 nSeg, u32 *segCounter, SeedScratch sc, SeedCaps cap,
-                                                            SeedOut out) {
+                                                            const u32 *segList, u32 nSeg, u32 *segCounter,
+                                                            SeedScratch sc, SeedCaps cap, SeedOut out) {
   __shared__ SeedSmem smem[kSeedWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   SeedSmem &sm   = smem[wib];
@@ -103,10 +103,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
   __syncwarp();
 
   while (true) {
-    u32 seg = 0;
-    if (lane == 0) seg = atomicAdd(segCounter, 1u);
-    seg = __shfl_sync(0xffffffffu, seg, 0);
-    if (seg >= nSeg) break;
+    u32 k = 0;
+    if (lane == 0) k = atomicAdd(segCounter, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= nSeg) break;
+    const u32 seg = segList ? segList[k] : k;   // segment = (ref index << 1) | strand
     nSegs++;
 
     const u32 sRead = segReads[seg >> 1];
@@ -313,11 +314,11 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
 
 }  // namespace
 
-void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, u32 nSeg, u32 *segCounter, SeedScratch sc,
-                 SeedCaps cap, int nWarps, SeedOut out, cudaStream_t st) {
+void launch_seed(ReadsDev R, TableDev T, DevParams P, const u32 *segReads, const u32 *segList, u32 nSeg,
+                 u32 *segCounter, SeedScratch sc, SeedCaps cap, int nWarps, SeedOut out, cudaStream_t st) {
   if (nSeg == 0) return;
   int blocks = (nWarps + kSeedWarps - 1) / kSeedWarps;
-  seed_kernel<<<blocks, kSeedThreads, 0, st>>>(R, T, P, segReads, nSeg, segCounter, sc, cap, out);
+  seed_kernel<<<blocks, kSeedThreads, 0, st>>>(R, T, P, segReads, segList, nSeg, segCounter, sc, cap, out);
   g_launches++;
 }
 
