@@ -28,6 +28,7 @@ EXPORTS = (
     "oic_default_params", "oic_create", "oic_destroy", "oic_set_reads", "oic_set_skip_kmers",
     "oic_load_hash_block", "oic_run_refs", "oic_run", "oic_num_overlaps", "oic_fetch_overlaps",
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
+    "oic_extend_batch_noalloc",
 )
 
 
@@ -93,6 +94,7 @@ def library():
         lib.oic_get_stats.argtypes = [vp, P(OicStats)]
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
+        lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
         lib.oic_last_error.argtypes = [vp]
         lib.oic_last_error.restype = ctypes.c_char_p
         _lib = lib

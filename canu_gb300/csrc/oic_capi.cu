@@ -13,6 +13,7 @@
 #include "oic_gpu.h"
 #include "oic_kernels.cuh"
 #include "oic_prims.cuh"
+#include "oic_internal.h"
 
 using namespace oic;
 
@@ -452,6 +453,25 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
 }
 
 }  // namespace
+
+namespace oic {
+
+int ctx_views(oic_ctx *ctx, CtxViews *v) {
+  if (!ctx || ctx->nReads == 0) return 1;
+  v->R      = ctx->R;
+  v->dp     = ctx->dp;
+  v->eml    = ctx->dEml.as<int>();
+  v->ctr32  = ctr32(ctx);
+  v->st     = ctx->st;
+  v->device = ctx->device;
+  return 0;
+}
+
+void ctx_set_error(oic_ctx *ctx, const char *msg) {
+  if (ctx) ctx->lastErr = msg;
+}
+
+}  // namespace oic
 
 // =================================================================================
 extern "C" {

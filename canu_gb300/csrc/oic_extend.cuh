@@ -1,11 +1,15 @@
-// oic_extend.cuh -- the batched Extend_Alignment kernel (one warp per problem).
+// oic_extend.cuh -- the batched Extend_Alignment kernel (one warp per problem),
+// shared by the allocating entry point (oic_pairs.cu) and the one that runs on a
+// static scratch array (oic_noalloc.cu).
 #pragma once
 
 #include "oic_kernels.cuh"
 
 namespace oic {
 
-template <int BANDW, int WARPS>
+// CHECK: validate each problem on the device (for problems the host has not seen)
+// and OR capacity flags into stats[2].
+template <int BANDW, int WARPS, bool CHECK = false>
 static __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) extend_batch_kernel(ReadsDev R, DevParams P, const int *eml,
                                                                   const ExtendProblem *probs, u32 n, WarpScratch scBase,
                                                                   AlignCaps cap, int *out, int *kind, int *deltaLen,
@@ -30,6 +34,16 @@ static __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) extend
 
   for (u64 i = gw; i < n; i += nw) {
     const ExtendProblem pb = probs[i];
+    // Problems are checked here too: a caller may hand them over in device memory.
+    if (CHECK && (pb.sRead >= R.nReads || pb.tRead >= R.nReads || pb.mLen < 1 || pb.mStart < 0 || pb.mOffset < 0 ||
+        (u64)pb.mStart + pb.mLen > R.len[pb.sRead] || (u64)pb.mOffset + pb.mLen > R.len[pb.tRead])) {
+      if (lane == 0) {
+        status[i] = kErrInternal;
+        kind[i]   = 0;
+        atomicOr((u32 *)(stats + 2), kErrInternal);
+      }
+      continue;
+    }
     const SeqView S = make_view(R, pb.sRead, pb.sRev ? 1 : 0);
     const SeqView T = make_view(R, pb.tRead, 0);
     const int sLen = (int)R.len[pb.sRead], tLen = (int)R.len[pb.tRead];
@@ -45,6 +59,7 @@ static __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) extend
       kind[i]        = k;
       deltaLen[i]    = w.leftLen;
       status[i]      = w.err;
+      if (CHECK && w.err) atomicOr((u32 *)(stats + 2), w.err);
     }
     __syncwarp();
   }

@@ -127,6 +127,28 @@ int oic_extend_batch(oic_ctx *ctx, uint32_t nAlign, const uint32_t *sRead, const
                      const uint32_t *tRead, const int32_t *mStart, const int32_t *mOffset,
                      const int32_t *mLen, int32_t *out, int32_t *kind, int32_t *deltaLen);
 
+/* One problem of oic_extend_batch_noalloc(), in device memory: 0-based read indices
+ * (ID - 1) of S (on strand sRev) and T, and the exact match (mStart in S, mOffset in
+ * T, mLen). */
+typedef struct oic_extend_problem {
+  uint32_t sRead, sRev, tRead;
+  int32_t  mStart, mOffset, mLen;
+} oic_extend_problem;
+
+/* No counterpart in the reference.  oic_extend_batch() for callers that cannot call
+ * cudaMalloc when they align -- code running under stream capture, programs whose
+ * memory pool owns the device, plugins with a fixed memory budget.  Problems and
+ * outputs are caller-owned DEVICE buffers (dOut: 5 per problem, as oic_extend_batch;
+ * dStatus: 0, or the capacity flag a problem hit).  The DP's scratch is a static
+ * device array of 23,072,768 bytes that every GPU loading the library holds until
+ * exit; the call allocates nothing.  Limit: each problem may keep at most 131072 DP
+ * cells and 8191 error rows per side of its seed match, otherwise the call returns
+ * OIC_ERR_OVERFLOW.  The first call on a device looks up the array's address (make it
+ * before any stream capture); calls that overlap on the GPU share the array and race.
+ * Runs on the context's stream and returns when the kernel has finished. */
+int oic_extend_batch_noalloc(oic_ctx *ctx, uint32_t nAlign, const oic_extend_problem *dProblems, int32_t *dOut,
+                             int32_t *dKind, int32_t *dDeltaLen, uint32_t *dStatus);
+
 /* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
  * min(n, table length) entries; *len gets the table length. */
 int oic_get_match_limit(oic_ctx *ctx, int32_t *dst, uint32_t n, uint32_t *len);
