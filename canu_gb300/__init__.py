@@ -62,7 +62,7 @@ class OicStats(ctypes.Structure):
         ("nHashBlocks", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
         ("msHash", ctypes.c_double), ("msSeed", ctypes.c_double),
         ("msAlign", ctypes.c_double), ("msTotal", ctypes.c_double),
-        ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64)]
+        ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64), ("dpCellsNoOverlap", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -19,6 +19,7 @@ namespace oic {
 struct WarpScratch {
   int  *arena;       // kept DP rows, band-compacted
   int4 *rowHdr;      // per error row: (arena offset, kept band left, kept band right, unused)
+  int  *rowsG;       // two row buffers of rowsGW ints in HBM, used once a band outgrows shared memory
   int  *deltaL;      // Left_Delta (merged delta of the last extension)
   int  *deltaR;      // Right_Delta
   int  *stack;       // Delta_Stack
@@ -30,6 +31,7 @@ struct AlignCaps {
   int rowCap;     // error rows per warp (also bounds the delta arrays)
   int nodeCap;    // match nodes per pair
   int bandW;      // ints per shared-memory row buffer
+  int rowsGW;     // ints per HBM row buffer (bands wider than bandW - 4 up to rowsGW - 4)
 };
 
 struct WarpDP {
@@ -48,6 +50,7 @@ static __device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &ba
   WarpScratch s;
   s.arena  = base.arena + gw * (u64)cap.arenaCap;
   s.rowHdr = base.rowHdr + gw * (u64)cap.rowCap;
+  s.rowsG  = base.rowsG ? base.rowsG + gw * (u64)(2 * cap.rowsGW) : nullptr;
   s.deltaL = base.deltaL + gw * (u64)(cap.rowCap + 8);
   s.deltaR = base.deltaR + gw * (u64)(cap.rowCap + 8);
   s.stack  = base.stack + gw * (u64)(cap.rowCap + 8);
@@ -169,6 +172,7 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
   // two diagonals on each side of the previous row's kept band are set to -2, as the
   // reference does (forward.C:150-153), so the neighbour reads need no bounds tests.
   int *prev = w.smA, *cur = w.smB;
+  int  bufW = w.cap.bandW;
   if (lane == 0) prev[2] = r0;
   __syncwarp();
 
@@ -181,7 +185,16 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
     if (e >= w.cap.rowCap) { w.err |= kErrRowsFull; return 0; }
     const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
     const int width = Rc - Lc + 1;
-    if (width + 4 > w.cap.bandW) { w.err |= kErrBandWide; return 0; }
+    if (width + 4 > bufW) {
+      // The band outgrew the shared-memory rows: continue in the warp's HBM rows.
+      if (bufW == w.cap.rowsGW || width + 4 > w.cap.rowsGW || !w.sc.rowsG) { w.err |= kErrBandWide; return 0; }
+      int *gA = w.sc.rowsG, *gB = w.sc.rowsG + w.cap.rowsGW;
+      for (int i = lane; i < bufW; i += 32) gA[i] = prev[i];
+      __syncwarp();
+      prev = gA;
+      cur  = gB;
+      bufW = w.cap.rowsGW;
+    }
 
     const int lim = w.eml[e];
     if (lane < 4) prev[(lane < 2 ? L - 2 + lane : R - 1 + lane) - prevBase + 2] = -2;
@@ -210,12 +223,18 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
 
     if (dEnd != INT_MAX) {
       w.cells += (unsigned long long)(dEnd - Lc + 1);
-      const int    row     = cv[dEnd];
-      const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
-      const int    tailLen = row - msLen;
-      const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
-      bool abort_ = (w.P.partial && score < maxScore);
-      if (e > 20 / 2 && tailLen >= 20 && slope >= w.P.minBranchTailSlope) abort_ = true;
+      const int row = cv[dEnd];
+      // Branch-point test in IEEE double on lane 0 (the FP64 pipe is narrow); lane 0
+      // holds maxScore, the other lanes take its decision.
+      int abort_ = 0;
+      if (lane == 0) {
+        const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
+        const int    tailLen = row - msLen;
+        const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
+        abort_ = (w.P.partial && score < maxScore) ||
+                 (e > 20 / 2 && tailLen >= 20 && slope >= w.P.minBranchTailSlope);
+      }
+      abort_ = __shfl_sync(0xffffffffu, abort_, 0);
       if (abort_) {
         aEnd = STEP * msLen;
         tEnd = STEP * (msLen + msD);
@@ -274,12 +293,19 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
       bestE   = e;
       // Score only moves up when Longest does: with Longest unchanged, rounding is
       // monotone, so Longest*BMV - e cannot pass the Max_Score of an earlier row.
-      const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
-      if (score > maxScore) {
-        maxScore = score;
-        msLen    = longest;
-        msD      = bestD;
-        msE      = bestE;
+      int u = 0;
+      if (lane == 0) {
+        const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
+        if (score > maxScore) {
+          maxScore = score;
+          u        = 1;
+        }
+      }
+      const bool upd = __shfl_sync(0xffffffffu, u, 0) != 0;
+      if (upd) {
+        msLen = longest;
+        msD   = bestD;
+        msE   = bestE;
       }
     }
 

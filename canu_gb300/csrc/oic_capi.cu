@@ -143,8 +143,8 @@ struct oic_ctx {
 
   // align
   DevBuf dWork, dRec, dCnt, dRecPos, dRecOut, dAlnOvf, dWorkK, dWorkK2, dWorkV2, dWorkScratch;
-  DevBuf dArena, dRowHdr, dDL, dDR, dStack, dAlive;        // normal
-  DevBuf dArena2, dRowHdr2, dDL2, dDR2, dStack2, dAlive2;  // wide
+  DevBuf dArena, dRowHdr, dDL, dDR, dStack, dAlive, dRowsG;         // normal
+  DevBuf dArena2, dRowHdr2, dDL2, dDR2, dStack2, dAlive2, dRowsG2;  // wide
   DevBuf dScanScratch;
 
   // counters (one small device block): [0..15] u32 counters, [16..] u64 stats
@@ -245,10 +245,11 @@ AlignConfig align_normal(const oic_ctx *c) {
   AlignConfig a;
   a.bandW         = 512;
   a.warps         = c->nSM * 3 * align_warps_per_block(512);
-  a.caps.arenaCap = 1 << 19;
+  a.caps.arenaCap = 1 << 20;
   a.caps.rowCap   = 1 << 14;
   a.caps.nodeCap  = 1 << 16;
   a.caps.bandW    = 512;
+  a.caps.rowsGW   = 16384;
   return a;
 }
 AlignConfig align_wide(const oic_ctx *c) {
@@ -259,6 +260,7 @@ AlignConfig align_wide(const oic_ctx *c) {
   a.caps.rowCap   = 1 << 18;
   a.caps.nodeCap  = 1 << 22;
   a.caps.bandW    = 8192;
+  a.caps.rowsGW   = 1 << 17;
   return a;
 }
 
@@ -266,18 +268,21 @@ int ensure_align_scratch(oic_ctx *ctx, const AlignConfig &ac, bool wide, WarpScr
   const size_t W = (size_t)ac.warps;
   DevBuf &ar = wide ? ctx->dArena2 : ctx->dArena;
   DevBuf &rh = wide ? ctx->dRowHdr2 : ctx->dRowHdr;
+  DevBuf &rg = wide ? ctx->dRowsG2 : ctx->dRowsG;
   DevBuf &dl = wide ? ctx->dDL2 : ctx->dDL;
   DevBuf &dr = wide ? ctx->dDR2 : ctx->dDR;
   DevBuf &sk = wide ? ctx->dStack2 : ctx->dStack;
   DevBuf &al = wide ? ctx->dAlive2 : ctx->dAlive;
   CK(ar.ensure(W * ac.caps.arenaCap * sizeof(int)));
   CK(rh.ensure(W * ac.caps.rowCap * sizeof(int4)));
+  CK(rg.ensure(W * 2 * (size_t)ac.caps.rowsGW * sizeof(int)));
   CK(dl.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(dr.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(sk.ensure(W * (ac.caps.rowCap + 8) * sizeof(int)));
   CK(al.ensure(W * ac.caps.nodeCap));
   s.arena  = ar.as<int>();
   s.rowHdr = rh.as<int4>();
+  s.rowsG  = rg.as<int>();
   s.deltaL = dl.as<int>();
   s.deltaR = dr.as<int>();
   s.stack  = sk.as<int>();
@@ -395,11 +400,21 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
     AlignConfig aw = align_wide(ctx);
     WarpScratch ww;
     if ((rc = ensure_align_scratch(ctx, aw, true, ww))) return rc;
+    cudaEvent_t w0, w1;
+    cudaEventCreate(&w0);
+    cudaEventCreate(&w1);
+    cudaEventRecord(w0, ctx->st);
     launch_align(aw.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
                  ctx->dWork.as<uint32_t>(), nOvf, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ww, aw.caps,
                  aw.warps, ao, ctx->st);
+    cudaEventRecord(w1, ctx->st);
     CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
     if ((rc = sync_check(ctx, "align kernel (wide)"))) return rc;
+    float wms = 0;
+    cudaEventElapsedTime(&wms, w0, w1);
+    cudaEventDestroy(w0);
+    cudaEventDestroy(w1);
+    if (verbose()) fprintf(stderr, "oic: wide DP pass %.2f ms\n", wms);
     if (h[cAlnOvf] > 0)
       return fail(ctx, OIC_ERR_OVERFLOW, "a read pair needs a wider DP band or deeper traceback than the engine holds (err 0x%x)",
                   h[cErr]);
@@ -449,6 +464,7 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   S.slideBases += st64[2 + kStSlides];
   S.extensions += st64[2 + kStExtensions];
   S.dpRows += st64[2 + kStRows];
+  S.dpCellsNoOverlap += st64[2 + kStCellsNoOlap];
   return OIC_OK;
 }
 
@@ -575,7 +591,8 @@ void oic_destroy(oic_ctx *ctx) {
                     &ctx->dDL,       &ctx->dDR,         &ctx->dStack,      &ctx->dAlive,     &ctx->dArena2,
                     &ctx->dRowHdr2,  &ctx->dDL2,       &ctx->dDR2,
                     &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr,
-                    &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch, &ctx->dSegList};
+                    &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch, &ctx->dSegList,
+                    &ctx->dRowsG,    &ctx->dRowsG2};
   for (DevBuf *b : bufs) b->release();
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;

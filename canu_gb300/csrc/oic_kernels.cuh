@@ -93,7 +93,7 @@ struct AlignOut {
 
 enum StatIdx {
   kStWithoutOlap = 0, kStWithOlap, kStSkipped, kStMulti, kStTotal, kStContained, kStDovetail,
-  kStCells, kStSlides, kStExtensions, kStRows, kStCount
+  kStCells, kStSlides, kStExtensions, kStRows, kStCellsNoOlap, kStCount
 };
 
 // bandW selects the shared-memory configuration (compiled instances: 512, 8192).

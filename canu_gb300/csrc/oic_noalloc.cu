@@ -83,11 +83,13 @@ extern "C" int oic_extend_batch_noalloc(oic_ctx *ctx, uint32_t nAlign, const oic
   sc.deltaR = (int *)(b + kNaArenaBytes + kNaRowBytes + kNaDeltaBytes);
   sc.stack  = (int *)(b + kNaArenaBytes + kNaRowBytes + 2 * kNaDeltaBytes);
   sc.alive  = nullptr;
+  sc.rowsG  = nullptr;
   AlignCaps cap;
   cap.arenaCap = kNaArenaCap;
   cap.rowCap   = kNaRowCap;
   cap.nodeCap  = 0;
   cap.bandW    = kNaBandW;
+  cap.rowsGW   = kNaBandW;
 
   // Counters in the context's preallocated block: [cells, slides, error flags].
   unsigned long long *stats = (unsigned long long *)v.ctr32 + 48;

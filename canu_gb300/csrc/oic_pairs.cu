@@ -437,9 +437,11 @@ __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(
     const PairRec pr = pairs[pi];
     u32 nRec = 0;
     w.err = 0;
+    const unsigned long long cellsBefore = w.cells;
     const bool ok = process_pair(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec);
     if (lane == 0) {
       if (ok) {
+        if (nRec == 0) ps.pc.v[kStCellsNoOlap] += w.cells - cellsBefore;
         out.cnt[pi] = nRec;
         for (int i = 0; i < kStCount; i++) ps.acc.v[i] += ps.pc.v[i];
       } else {

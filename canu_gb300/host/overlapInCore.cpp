@@ -268,10 +268,11 @@ int main(int argc, char **argv) {
   fprintf(S, " Rejected by long window = %ld\n", (long)st.badLongWindow);
   if (S != stderr) fclose(S);
 
-  fprintf(stderr, "GPU: %lu overlaps; %lu seeds, %lu pairs, %lu extensions, %lu DP cells; hash %.2f ms, seed %.2f ms, "
-                  "align %.2f ms, total %.2f ms\n",
+  fprintf(stderr, "GPU: %lu overlaps; %lu seeds, %lu pairs, %lu extensions, %lu DP cells (%lu in pairs without "
+                  "overlap), %lu rows; hash %.2f ms, seed %.2f ms, align %.2f ms, total %.2f ms\n",
           (unsigned long)n, (unsigned long)st.seeds, (unsigned long)st.candidatePairs, (unsigned long)st.extensions,
-          (unsigned long)st.dpCells, st.msHash, st.msSeed, st.msAlign, st.msTotal);
+          (unsigned long)st.dpCells, (unsigned long)st.dpCellsNoOverlap, (unsigned long)st.dpRows, st.msHash,
+          st.msSeed, st.msAlign, st.msTotal);
   fprintf(stderr, "Bye.\n");
   oic_seqdb_free(&db);
   return 0;

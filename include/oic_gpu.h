@@ -67,6 +67,7 @@ typedef struct oic_stats {
   double   msHash, msSeed, msAlign, msTotal;       /* device time (CUDA events) of oic_run work */
   double   msReads;                                /* device time of the last oic_set_reads */
   uint64_t kernelLaunches;                         /* kernels launched by oic_run and its parts */
+  uint64_t dpCellsNoOverlap;                       /* DP cells spent on pairs that emitted nothing */
 } oic_stats;
 
 typedef struct oic_ctx oic_ctx;
