@@ -28,8 +28,21 @@ EXPORTS = (
     "oic_default_params", "oic_create", "oic_destroy", "oic_set_reads", "oic_set_skip_kmers",
     "oic_load_hash_block", "oic_run_refs", "oic_run", "oic_num_overlaps", "oic_fetch_overlaps",
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
-    "oic_extend_batch_noalloc",
+    "oic_extend_batch_noalloc", "oic_set_filter", "oic_collect_pairs", "oic_num_pairs", "oic_get_pairs",
+    "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam",
 )
+
+# Learned candidate filter (include/oic_gpu.h): feature row width, hidden width and the
+# FP16 parameter array w1[128][80] | b1[128] | w2[128][128] | b2[128] | w3[128] | b3.
+FILTER_FEATURES, FILTER_IN, FILTER_HIDDEN = 67, 80, 128
+FILTER_OFFSETS = {"w1": (0, (128, 80)), "b1": (10240, (128,)), "w2": (10368, (128, 128)),
+                  "b2": (26752, (128,)), "w3": (26880, (128,)), "b3": (27008, (1,))}
+FILTER_NPARAM = 27009
+
+# oic_pair_info
+PAIR_DTYPE = np.dtype([("aID", "<u4"), ("bID", "<u4"), ("flags", "<u4"), ("seeds", "<u4"), ("nodes", "<u4"),
+                       ("overlaps", "<u4"), ("cells", "<u4"), ("score", "<f4"), ("extensions", "<u4"),
+                       ("firstHit", "<i4"), ("cellsFirst", "<u4"), ("extLimit", "<u4")])
 
 
 class OicError(RuntimeError):
@@ -62,7 +75,8 @@ class OicStats(ctypes.Structure):
         ("nHashBlocks", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
         ("msHash", ctypes.c_double), ("msSeed", ctypes.c_double),
         ("msAlign", ctypes.c_double), ("msTotal", ctypes.c_double),
-        ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64), ("dpCellsNoOverlap", ctypes.c_uint64)]
+        ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64), ("dpCellsNoOverlap", ctypes.c_uint64),
+        ("filteredPairs", ctypes.c_uint64), ("msFilter", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -95,6 +109,15 @@ def library():
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
+        lib.oic_set_filter.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
+        lib.oic_collect_pairs.argtypes = [vp, ctypes.c_int]
+        lib.oic_num_pairs.argtypes = [vp, P(U64), P(U64)]
+        lib.oic_get_pairs.argtypes = [vp, vp, vp, vp, U64, U64]
+        lib.oic_clear_pairs.argtypes = [vp]
+        lib.oic_mlp_forward.argtypes = [vp, vp, U32, vp, vp, vp, vp]
+        lib.oic_mlp_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, U32, vp, vp, vp, vp, vp]
+        F = ctypes.c_float
+        lib.oic_mlp_adam.argtypes = [vp, vp, vp, vp, vp, F, F, F, F, F, F, U32, vp]
         lib.oic_last_error.argtypes = [vp]
         lib.oic_last_error.restype = ctypes.c_char_p
         _lib = lib
@@ -228,6 +251,36 @@ class Overlapper:
         self._check(self._lib.oic_get_match_limit(self._ctx, _ptr(out), n.value, ctypes.byref(n)))
         return out
 
+    def set_filter(self, params, threshold, full_threshold=0.0):
+        """Learned candidate filter: params = FILTER_NPARAM float16 values (None: off).
+        Pairs scored below threshold are dropped; below full_threshold they stop after a
+        first extension that found no overlap."""
+        if params is None:
+            self._check(self._lib.oic_set_filter(self._ctx, None, 0.0, 0.0))
+            return
+        prm = np.ascontiguousarray(params, dtype=np.float16).view(np.uint16)
+        if prm.size != FILTER_NPARAM:
+            raise ValueError(f"filter needs {FILTER_NPARAM} parameters, got {prm.size}")
+        self._check(self._lib.oic_set_filter(self._ctx, _ptr(prm), float(threshold), float(full_threshold)))
+
+    def collect_pairs(self, mode=1):
+        """0 off, 1 candidate pairs + feature rows, 2 also their match runs."""
+        self._check(self._lib.oic_collect_pairs(self._ctx, int(mode)))
+
+    def pairs(self, nodes=False):
+        """Collected pairs: (info [PAIR_DTYPE], feature rows [n, 80] float16[, runs [m, 3] int32])."""
+        n, m = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._lib.oic_num_pairs(self._ctx, ctypes.byref(n), ctypes.byref(m)))
+        info = np.zeros(n.value, dtype=PAIR_DTYPE)
+        feat = np.zeros((n.value, FILTER_IN), dtype=np.float16)
+        runs = np.zeros((m.value if nodes else 0, 3), dtype=np.int32)
+        self._check(self._lib.oic_get_pairs(self._ctx, _ptr(info), _ptr(feat), _ptr(runs) if nodes else None,
+                                            n.value, m.value if nodes else 0))
+        return (info, feat, runs) if nodes else (info, feat)
+
+    def clear_pairs(self):
+        self._check(self._lib.oic_clear_pairs(self._ctx))
+
     def extend_batch(self, sRead, sRev, tRead, mStart, mOffset, mLen):
         """Batched Extend_Alignment; returns (out[n,5], kind[n], deltaLen[n])."""
         a = [np.ascontiguousarray(x, dtype=t) for x, t in zip(
@@ -239,6 +292,28 @@ class Overlapper:
         dl = np.zeros(n, dtype=np.int32)
         self._check(self._lib.oic_extend_batch(self._ctx, n, *[_ptr(x) for x in a], _ptr(out), _ptr(kind), _ptr(dl)))
         return out, kind, dl
+
+
+def _mlp_check(rc, what):
+    if rc != OIC_OK:
+        raise OicError(rc, what + " failed")
+
+
+def mlp_forward(params, x, n, logit, h1=0, h2=0, stream=0):
+    """oic_mlp_forward on device pointers (ints)."""
+    _mlp_check(library().oic_mlp_forward(params, x, n, logit, h1 or None, h2 or None, stream or None), "mlp forward")
+
+
+def mlp_backward(params, x, h1, h2, logit, label, weight, n, grad, g1, g2, loss=0, stream=0):
+    """oic_mlp_backward on device pointers (ints); weight/loss may be 0 (NULL)."""
+    _mlp_check(library().oic_mlp_backward(params, x, h1, h2, logit, label, weight or None, n, grad, g1, g2,
+                                          loss or None, stream or None), "mlp backward")
+
+
+def mlp_adam(master, m, v, grad, params, lr, beta1, beta2, eps, grad_scale, weight_decay, step, stream=0):
+    """oic_mlp_adam on device pointers (ints)."""
+    _mlp_check(library().oic_mlp_adam(master, m, v, grad, params, lr, beta1, beta2, eps, grad_scale, weight_decay,
+                                      step, stream or None), "mlp adam")
 
 
 def sort_records(rec):

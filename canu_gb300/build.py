@@ -26,7 +26,8 @@ INC = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
            "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
-CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu", "oic_noalloc.cu"]
+CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu", "oic_noalloc.cu",
+              "oic_filter.cu"]
 
 
 def nvcc():

@@ -150,6 +150,17 @@ struct oic_ctx {
   // counters (one small device block): [0..15] u32 counters, [16..] u64 stats
   DevBuf dCtr;
 
+  // learned candidate filter
+  bool   filterOn       = false;
+  float  filterLogitThr = 0.0f;      // drop below
+  float  filterTierThr  = -INFINITY; // single-extension tier below
+  DevBuf dFilterPrm, dFeat, dLogit, dPairCells, dPairExt;
+  cudaEvent_t evF0 = nullptr, evF1 = nullptr;
+  int    collect = 0;                      // 0 off, 1 pairs + features, 2 also match runs
+  std::vector<oic_pair_info> colInfo;
+  std::vector<uint16_t>      colFeat;
+  std::vector<int32_t>       colNodes;
+
   std::vector<uint32_t> out;   // accumulated records, 6 words each
   oic_stats stats{};
 };
@@ -159,7 +170,7 @@ namespace {
 constexpr int kRetrySmaller = 100;   // run_batch: the batch's output did not fit
 
 enum CtrIdx {   // u32 counters
-  cSegCounter = 0, cPairCount, cNodeCount, cSegOvf, cWorkCounter, cAlnOvf, cErr, cRecTotal, cNumU32 = 16
+  cSegCounter = 0, cPairCount, cNodeCount, cSegOvf, cWorkCounter, cAlnOvf, cErr, cRecTotal, cKeep, cNumU32 = 16
 };
 constexpr int kSeedStatBase  = 16;   // u64 index: [seeds, segments]
 constexpr int kAlignStatBase = 20;   // u64 index: kStCount entries
@@ -298,6 +309,57 @@ int sync_check(oic_ctx *ctx, const char *where) {
   return OIC_OK;
 }
 
+// Append the batch's candidate pairs (and their feature rows and match runs) to the
+// context's collection.
+int collect_batch(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, bool filtered) {
+  std::vector<PairRec>  pr(nPairs);
+  std::vector<uint32_t> cnt(nPairs), cells(nPairs);
+  std::vector<float>    logit(nPairs);
+  std::vector<int4>     ext(nPairs);
+  CK(cudaMemcpyAsync(ext.data(), ctx->dPairExt.p, (size_t)nPairs * sizeof(int4), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(pr.data(), ctx->dPairs.p, (size_t)nPairs * sizeof(PairRec), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(cnt.data(), ctx->dCnt.p, (size_t)nPairs * 4, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(cells.data(), ctx->dPairCells.p, (size_t)nPairs * 4, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(logit.data(), ctx->dLogit.p, (size_t)nPairs * 4, cudaMemcpyDeviceToHost, ctx->st));
+  const size_t f0 = ctx->colFeat.size();
+  ctx->colFeat.resize(f0 + (size_t)nPairs * OIC_FILTER_IN);
+  CK(cudaMemcpyAsync(ctx->colFeat.data() + f0, ctx->dFeat.p, (size_t)nPairs * OIC_FILTER_IN * 2,
+                     cudaMemcpyDeviceToHost, ctx->st));
+  std::vector<int4> nodes;
+  if (ctx->collect >= 2) {
+    nodes.resize(nNodes);
+    CK(cudaMemcpyAsync(nodes.data(), ctx->dNodes.p, (size_t)nNodes * sizeof(int4), cudaMemcpyDeviceToHost, ctx->st));
+  }
+  int rc = sync_check(ctx, "pair collection");
+  if (rc) return rc;
+  const size_t i0 = ctx->colInfo.size();
+  ctx->colInfo.resize(i0 + nPairs);
+  for (uint32_t p = 0; p < nPairs; p++) {
+    oic_pair_info &q = ctx->colInfo[i0 + p];
+    q.aID      = pr[p].sRead + 1;
+    q.bID      = ctx->blkFirst + pr[p].tStr;
+    const bool dropped = filtered && logit[p] < ctx->filterLogitThr;
+    q.flags    = (pr[p].flags & 1u) | (dropped ? 2u : 0u);
+    q.seeds    = (uint32_t)pr[p].diagCt;
+    q.nodes    = pr[p].nodeCnt;
+    q.overlaps = cnt[p];
+    q.cells    = cells[p];
+    q.score    = logit[p];
+    q.extensions = (uint32_t)ext[p].x;
+    q.firstHit   = ext[p].y;
+    q.cellsFirst = (uint32_t)ext[p].z;
+    q.extLimit   = (uint32_t)ext[p].w;
+    if (ctx->collect >= 2)
+      for (uint32_t j = 0; j < pr[p].nodeCnt; j++) {
+        const int4 &nd = nodes[pr[p].nodeOff + j];
+        ctx->colNodes.push_back(nd.x);
+        ctx->colNodes.push_back(nd.y);
+        ctx->colNodes.push_back(nd.z);
+      }
+  }
+  return OIC_OK;
+}
+
 // Process one batch of eligible ref reads against the loaded block.  Returns OIC_OK,
 // or OIC_ERR_OVERFLOW when the batch's output did not fit (caller splits the batch).
 int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
@@ -357,6 +419,26 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   const uint32_t nPairs = h[cPairCount];
   const uint32_t nNodes = h[cNodeCount];
 
+  // Learned filter: feature rows of every candidate pair, then their scores.
+  const bool useFilter = ctx->filterOn && nPairs > 0;
+  if ((useFilter || ctx->collect) && nPairs) {
+    if (!ctx->evF0) {
+      CK(cudaEventCreate(&ctx->evF0));
+      CK(cudaEventCreate(&ctx->evF1));
+    }
+    CK(cudaEventRecord(ctx->evF0, ctx->st));
+    CK(ctx->dFeat.ensure((size_t)nPairs * OIC_FILTER_IN * 2));
+    launch_pair_features(ctx->dPairs.as<PairRec>(), nPairs, ctx->dNodes.as<int4>(), ctx->R.len, ctx->T.sread,
+                         ctx->dp.kmerLen, ctx->dFeat.p, ctx->st);
+    CK(ctx->dLogit.ensure((size_t)nPairs * sizeof(float)));
+    if (useFilter)
+      CK(launch_mlp_forward(ctx->dFilterPrm.p, ctx->dFeat.p, nPairs, ctx->dLogit.as<float>(), nullptr, nullptr,
+                            ctx->st));
+    else
+      CK(cudaMemsetAsync(ctx->dLogit.p, 0, (size_t)nPairs * sizeof(float), ctx->st));
+    CK(cudaEventRecord(ctx->evF1, ctx->st));
+  }
+
   // Align every pair.
   CK(ctx->dWork.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
   CK(ctx->dCnt.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
@@ -369,11 +451,24 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
     CK(ctx->dWorkK2.ensure((size_t)nPairs * 8));
     CK(ctx->dWorkV2.ensure((size_t)nPairs * 4));
     CK(ctx->dWorkScratch.ensure(radix_sort_scratch(nPairs) + 256));
-    launch_work_keys(ctx->dPairs.as<PairRec>(), nPairs, ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->st);
+    launch_work_keys(ctx->dPairs.as<PairRec>(), nPairs, useFilter ? ctx->dLogit.as<float>() : nullptr,
+                     ctx->filterLogitThr, ctr32(ctx) + cKeep, ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(),
+                     ctx->st);
     CK(radix_sort_u64_u32(ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->dWorkK2.as<u64>(),
                           ctx->dWorkV2.as<uint32_t>(), nPairs, 32, ctx->dWorkScratch.p, ctx->st));
   }
   if (nPairs) CK(cudaMemsetAsync(ctx->dCnt.p, 0, nPairs * sizeof(uint32_t), ctx->st));
+  uint32_t nWork = nPairs;
+  if (useFilter) {   // the kept pairs lead the sorted work list
+    CK(cudaMemcpyAsync(&nWork, ctr32(ctx) + cKeep, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = sync_check(ctx, "candidate filter"))) return rc;
+  }
+  if (ctx->collect && nPairs) {
+    CK(ctx->dPairCells.ensure((size_t)nPairs * sizeof(uint32_t)));
+    CK(ctx->dPairExt.ensure((size_t)nPairs * sizeof(int4)));
+    CK(cudaMemsetAsync(ctx->dPairCells.p, 0, (size_t)nPairs * sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctx->dPairExt.p, 0, (size_t)nPairs * sizeof(int4), ctx->st));
+  }
   AlignOut ao;
   ao.rec           = ctx->dRec.as<uint32_t>();
   ao.cnt           = ctx->dCnt.as<uint32_t>();
@@ -381,11 +476,16 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   ao.overflowCount = ctr32(ctx) + cAlnOvf;
   ao.stats         = ctr64(ctx) + kAlignStatBase;
   ao.err           = ctr32(ctx) + cErr;
+  ao.cells         = (ctx->collect && nPairs) ? ctx->dPairCells.as<uint32_t>() : nullptr;
+  ao.ext           = (ctx->collect && nPairs) ? ctx->dPairExt.as<int4>() : nullptr;
+  const bool tier  = useFilter && ctx->filterTierThr > ctx->filterLogitThr;
+  ao.tierLogit     = tier ? ctx->dLogit.as<float>() : nullptr;
+  ao.tierThr       = ctx->filterTierThr;
   AlignConfig an = align_normal(ctx);
   WarpScratch ws;
   if ((rc = ensure_align_scratch(ctx, an, false, ws))) return rc;
   launch_align(an.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
-               ctx->dWork.as<uint32_t>(), nPairs, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, an.caps,
+               ctx->dWork.as<uint32_t>(), nWork, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, an.caps,
                an.warps, ao, ctx->st);
   CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
   if ((rc = sync_check(ctx, "align kernel"))) return rc;
@@ -448,6 +548,12 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   cudaEventElapsedTime(&b, evSeed1, evAln1);
   msSeed += a;
   msAlign += b;
+  if ((useFilter || ctx->collect) && nPairs) {
+    float f = 0;
+    cudaEventElapsedTime(&f, ctx->evF0, ctx->evF1);
+    ctx->stats.msFilter += f;
+  }
+  if (ctx->collect && nPairs && (rc = collect_batch(ctx, nPairs, nNodes, useFilter))) return rc;
 
   oic_stats &S = ctx->stats;
   S.seeds += st64[0];
@@ -465,6 +571,7 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   S.extensions += st64[2 + kStExtensions];
   S.dpRows += st64[2 + kStRows];
   S.dpCellsNoOverlap += st64[2 + kStCellsNoOlap];
+  if (useFilter) S.filteredPairs += nPairs - nWork;
   return OIC_OK;
 }
 
@@ -592,8 +699,11 @@ void oic_destroy(oic_ctx *ctx) {
                     &ctx->dRowHdr2,  &ctx->dDL2,       &ctx->dDR2,
                     &ctx->dStack2,   &ctx->dAlive2,     &ctx->dScanScratch, &ctx->dCtr,
                     &ctx->dWorkK,    &ctx->dWorkK2,     &ctx->dWorkV2,     &ctx->dWorkScratch, &ctx->dSegList,
-                    &ctx->dRowsG,    &ctx->dRowsG2};
+                    &ctx->dRowsG,    &ctx->dRowsG2,     &ctx->dFilterPrm,  &ctx->dFeat,      &ctx->dLogit,
+                    &ctx->dPairCells, &ctx->dPairExt};
   for (DevBuf *b : bufs) b->release();
+  if (ctx->evF0) cudaEventDestroy(ctx->evF0);
+  if (ctx->evF1) cudaEventDestroy(ctx->evF1);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -1011,6 +1121,62 @@ int oic_clear_overlaps(oic_ctx *ctx) {
 int oic_get_stats(oic_ctx *ctx, oic_stats *st) {
   if (!ctx || !st) return OIC_ERR_ARG;
   *st = ctx->stats;
+  return OIC_OK;
+}
+
+int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (!params) {
+    ctx->filterOn = false;
+    return OIC_OK;
+  }
+  if (!(threshold >= 0.0f && threshold < 1.0f) || !(fullThreshold >= 0.0f && fullThreshold < 1.0f))
+    return fail(ctx, OIC_ERR_ARG, "filter thresholds must be in [0, 1)");
+  cudaSetDevice(ctx->device);
+  CK(ctx->dFilterPrm.ensure(OIC_FILTER_NPARAM * sizeof(uint16_t)));
+  CK(cudaMemcpyAsync(ctx->dFilterPrm.p, params, OIC_FILTER_NPARAM * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                     ctx->st));
+  int rc = sync_check(ctx, "filter upload");
+  if (rc) return rc;
+  // sigmoid(z) < t  <=>  z < ln(t / (1 - t)); t = 0 keeps every pair.
+  auto logit = [](float t) {
+    return t > 0.0f ? (float)std::log((double)t / (1.0 - (double)t)) : -INFINITY;
+  };
+  ctx->filterLogitThr = logit(threshold);
+  ctx->filterTierThr  = logit(fullThreshold);
+  ctx->filterOn       = true;
+  return OIC_OK;
+}
+
+int oic_collect_pairs(oic_ctx *ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 2) return OIC_ERR_ARG;
+  ctx->collect = mode;
+  return OIC_OK;
+}
+
+int oic_num_pairs(oic_ctx *ctx, uint64_t *nPairs, uint64_t *nNodes) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (nPairs) *nPairs = ctx->colInfo.size();
+  if (nNodes) *nNodes = ctx->colNodes.size() / 3;
+  return OIC_OK;
+}
+
+int oic_get_pairs(oic_ctx *ctx, oic_pair_info *info, uint16_t *feat, int32_t *nodes, uint64_t maxPairs,
+                  uint64_t maxNodes) {
+  if (!ctx) return OIC_ERR_ARG;
+  const uint64_t np = std::min<uint64_t>(maxPairs, ctx->colInfo.size());
+  const uint64_t nn = std::min<uint64_t>(maxNodes, ctx->colNodes.size() / 3);
+  if (info) memcpy(info, ctx->colInfo.data(), np * sizeof(oic_pair_info));
+  if (feat) memcpy(feat, ctx->colFeat.data(), np * OIC_FILTER_IN * sizeof(uint16_t));
+  if (nodes) memcpy(nodes, ctx->colNodes.data(), nn * 3 * sizeof(int32_t));
+  return OIC_OK;
+}
+
+int oic_clear_pairs(oic_ctx *ctx) {
+  if (!ctx) return OIC_ERR_ARG;
+  std::vector<oic_pair_info>().swap(ctx->colInfo);
+  std::vector<uint16_t>().swap(ctx->colFeat);
+  std::vector<int32_t>().swap(ctx->colNodes);
   return OIC_OK;
 }
 

@@ -89,6 +89,11 @@ struct AlignOut {
   u32 *overflowCount;
   unsigned long long *stats;   // see StatIdx
   u32 *err;
+  u32 *cells;           // optional: DP cells spent on each pair slot (saturating) ...
+  int4 *ext;            // ... and (extensions, first extension with an overlap or -1,
+                        //      cells of the first extension, extension limit applied)
+  const float *tierLogit;   // optional: pairs scored below tierThr stop after their first
+  float        tierThr;     // extension when it found no overlap
 };
 
 enum StatIdx {
@@ -109,8 +114,19 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
                          WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
                          unsigned long long *stats, cudaStream_t st);
 
-// Sort keys that put the pairs with the most match nodes first.
-void launch_work_keys(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals, cudaStream_t st);
+// Sort keys that put the pairs with the most match nodes first.  With a filter score
+// (logit non-null) a pair whose score is below logitThr gets the largest key, so the
+// kept pairs come first; keepCount (zeroed by the caller) gets their number.
+void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
+                      unsigned long long *keys, u32 *vals, cudaStream_t st);
+
+// ---------------- learned candidate filter (oic_filter.cu) ----------------
+// feat: n x 80 FP16 rows (67 features, 13 zeros) of the candidate pairs.
+void launch_pair_features(const PairRec *pairs, u32 n, const int4 *nodes, const u32 *readLen, const u32 *strRead,
+                          int K, void *feat, cudaStream_t st);
+// logit[i] of every row of X (n x 80 FP16); H1/H2 (n x 128 FP16) written when non-null.
+cudaError_t launch_mlp_forward(const void *prm, const void *X, u32 n, float *logit, void *H1, void *H2,
+                               cudaStream_t st);
 
 // Compact per-pair record slots into a dense record array.
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st);

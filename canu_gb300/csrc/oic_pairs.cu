@@ -183,6 +183,9 @@ struct PairCounts {
 struct PairSmem {
   Olap               olap[kMaxDistinct];
   int                nOlap;
+  int                nExt;       // extensions run for the pair in flight
+  int                firstHit;   // index of its first extension that added an overlap, -1 none
+  unsigned long long cellsFirst; // DP cells of its first extension
   PairCounts         pc;    // counts of the pair in flight
   PairCounts         acc;   // committed counts of the warp
 };
@@ -244,13 +247,16 @@ __device__ void output_partial(u32 *dst, u32 sID, u32 tID, int rev, const Olap &
 // Process_Matches for one pair.  Counts go to ps.pc, records (lane 0) to recOut.
 // Returns false on a capacity overflow: the caller then discards ps.pc and the records.
 __device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const TableDev &Tb, const PairRec &pr,
-                             const int4 *nodesAll, u32 *recOut, u32 &nRec) {
+                             const int4 *nodesAll, u32 *recOut, u32 &nRec, int extLimit) {
   const int lane = threadIdx.x & 31;
   const DevParams &P = w.P;
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < kStCount; i++) ps.pc.v[i] = 0;
-    ps.nOlap = 0;
+    ps.nOlap      = 0;
+    ps.nExt       = 0;
+    ps.firstHit   = -1;
+    ps.cellsFirst = 0;
   }
   __syncwarp();
   nRec = 0;
@@ -349,14 +355,26 @@ __device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const T
     const bool dov = (kind == kDovetail) || P.partial;
     if (lane == 0) {
       ps.pc.v[kStExtensions]++;
+      bool added = false;
       if (dov && 1 + sHi - sLo >= P.minOlapLen && 1 + tHi - tLo >= P.minOlapLen) {
         const int    olapLen = 1 + min(sHi - sLo, tHi - tLo);
         const double quality = __ddiv_rn((double)errors, (double)olapLen);
-        if (errors <= error_bound(olapLen, P.maxErate))
+        if (errors <= error_bound(olapLen, P.maxErate)) {
           add_overlap(P.partial, sLo, sHi, tLo, tHi, quality, w.leftLen, ps.olap, ps.nOlap);
+          added = true;
+        }
       }
+      if (ps.nExt == 0) ps.cellsFirst = w.cells - cells0;
+      if (added && ps.firstHit < 0) ps.firstHit = ps.nExt;
+      ps.nExt++;
     }
     if (cons) break;
+    // Early exit (learned filter's single-extension tier): stop once extLimit
+    // extensions have run without an overlap.
+    if (extLimit > 0) {
+      __syncwarp();
+      if (ps.nExt >= extLimit && ps.nOlap == 0) break;
+    }
 
     // Drop the longest match and every match that lies on the alignment (:476-490).
     for (int i = lane; i < cnt; i += 32) {
@@ -438,11 +456,19 @@ __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(
     u32 nRec = 0;
     w.err = 0;
     const unsigned long long cellsBefore = w.cells;
-    const bool ok = process_pair(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec);
+    int extLimit = 0;   // 0: every match node may be extended (the reference's rule)
+    if (out.tierLogit && out.tierLogit[pi] < out.tierThr) extLimit = 1;
+    const bool ok = process_pair(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, extLimit);
     if (lane == 0) {
       if (ok) {
         if (nRec == 0) ps.pc.v[kStCellsNoOlap] += w.cells - cellsBefore;
         out.cnt[pi] = nRec;
+        if (out.cells) {
+          const unsigned long long c = w.cells - cellsBefore;
+          out.cells[pi] = c > 0xffffffffull ? 0xffffffffu : (u32)c;
+          out.ext[pi]   = make_int4(ps.nExt, ps.firstHit,
+                                    ps.cellsFirst > 0x7fffffffull ? 0x7fffffff : (int)ps.cellsFirst, extLimit);
+        }
         for (int i = 0; i < kStCount; i++) ps.acc.v[i] += ps.pc.v[i];
       } else {
         out.cnt[pi] = 0;
@@ -464,11 +490,23 @@ __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(
   }
 }
 
-// Longest work first: key = ~(match nodes of the pair), value = pair index.
-__global__ void work_keys_kernel(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals) {
-  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    keys[i] = 0xffffffffull - (unsigned long long)pairs[i].nodeCnt;
-    vals[i] = i;
+// Longest work first: key = ~(match nodes of the pair), value = pair index.  Pairs
+// the filter drops get key 0xffffffff (every kept pair has at least one node).
+__global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
+                                 unsigned long long *keys, u32 *vals) {
+  const u32 stride = gridDim.x * blockDim.x;
+  for (u32 i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+    const u32 i    = i0 + threadIdx.x;
+    bool      keep = false;
+    if (i < n) {
+      keep    = !logit || !(logit[i] < logitThr);
+      keys[i] = keep ? 0xffffffffull - (unsigned long long)pairs[i].nodeCnt : 0xffffffffull;
+      vals[i] = i;
+    }
+    if (logit) {
+      const unsigned b = __ballot_sync(0xffffffffu, keep);
+      if ((threadIdx.x & 31) == 0 && b) atomicAdd(keepCount, (u32)__popc(b));
+    }
   }
 }
 
@@ -530,11 +568,12 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
   }
 }
 
-void launch_work_keys(const PairRec *pairs, u32 n, unsigned long long *keys, u32 *vals, cudaStream_t st) {
+void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
+                      unsigned long long *keys, u32 *vals, cudaStream_t st) {
   if (n == 0) return;
   unsigned g = (n + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
-  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, keys, vals);
+  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, keepCount, keys, vals);
   g_launches++;
 }
 

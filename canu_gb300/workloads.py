@@ -9,7 +9,8 @@ run with.  Sizes follow the benchmark configurations of the overlap stage:
       tandem arrays of a 171 bp unit (2% divergence); 30x HiFi-like reads (normal,
       mean 15 kb, sd 3 kb), 0.5% errors, k=22, --minlength 1000, --maxerate 0.01,
       --hashbits 25, --hashdatalen 1.6 Gbp; with a frequent-k-mer skip list (k-mers of
-      genome multiplicity > 10, i.e. read count > 10x coverage)
+      genome multiplicity > 10, i.e. read count > 10x coverage).  Seed 6: the learned
+      filter trains on seeds 1-5 of this shape and is evaluated on seed 6.
   c3  20 Mbp iid genome, 25x Pareto reads (alpha 1.5, min 500, cap 100 kb), 5% errors
       (1:2:2), --minlength 500, --maxerate 0.12, --hashbits 24
   c5  200 Mbp genome with 1000 x 6 kb repeats and 3% tandem arrays, 40x c2-like reads,
@@ -34,7 +35,7 @@ WORKLOADS = {
     "c2": dict(
         synth=dict(genome=50_000_000, coverage=30, len_dist="normal", len_mean=15000, len_sd=3000, len_min=1000,
                    len_max=30000, err=0.005, ratio="1:1:1", repeat_copies=200, repeat_len=6000, repeat_div=0.01,
-                   tandem_frac=0.02, tandem_unit=171, tandem_div=0.02, seed=2),
+                   tandem_frac=0.02, tandem_unit=171, tandem_div=0.02, seed=6),
         params=dict(kmerLen=22, hashBits=25, maxErate=0.01, minOlapLen=1000, maxHashDataLen=1_600_000_000,
                     numThreads=8),
         skip=True, skip_min_count=11),

@@ -68,6 +68,8 @@ typedef struct oic_stats {
   double   msReads;                                /* device time of the last oic_set_reads */
   uint64_t kernelLaunches;                         /* kernels launched by oic_run and its parts */
   uint64_t dpCellsNoOverlap;                       /* DP cells spent on pairs that emitted nothing */
+  uint64_t filteredPairs;                          /* candidate pairs the learned filter dropped */
+  double   msFilter;                               /* device time of features + filter inference */
 } oic_stats;
 
 typedef struct oic_ctx oic_ctx;
@@ -149,6 +151,82 @@ typedef struct oic_extend_problem {
  * Runs on the context's stream and returns when the kernel has finished. */
 int oic_extend_batch_noalloc(oic_ctx *ctx, uint32_t nAlign, const oic_extend_problem *dProblems, int32_t *dOut,
                              int32_t *dKind, int32_t *dDeltaLen, uint32_t *dStatus);
+
+/* ---------------------------------------------------------------------------------
+ * Learned candidate filter.  No counterpart in the reference: overlapInCore extends
+ * every candidate pair that passes its hopeless check (overlapInCore-Process_String_
+ * Overlaps.C:354-547).  With a filter set, a small MLP scores each candidate pair from
+ * its seeds before the DP, and pairs scored below the threshold are not extended.
+ * Every record still comes from the exact DP, so the output is a subset of the plain
+ * output (recall < 1 is possible, wrong records are not).
+ *
+ * Feature row of a pair (FP16, OIC_FILTER_IN values): 64 bins of seed density over
+ * the pair's diagonals (-lenS, lenT) -- seeds in the bin / overlap length along the
+ * bin's centre diagonal (at least 64), capped at 4 -- then (ln lenS - 8)/2,
+ * (ln lenT - 8)/2, (ln(1 + seeds) - 5)/4, then 13 zeros.
+ * Network: 80 -> 128 ReLU -> 128 ReLU -> 1 (logit), FP16 parameters and activations,
+ * FP32 accumulation.  Parameter array (OIC_FILTER_NPARAM FP16 values, row-major
+ * [out][in]): w1[128][80] | b1[128] | w2[128][128] | b2[128] | w3[128] | b3.
+ * --------------------------------------------------------------------------------- */
+#define OIC_FILTER_FEATURES 67
+#define OIC_FILTER_IN       80
+#define OIC_FILTER_HIDDEN   128
+#define OIC_FILTER_NPARAM   27009
+
+/* One candidate pair seen by a run while pair collection is on. */
+typedef struct oic_pair_info {
+  uint32_t aID;        /* ref read (S), 1-based */
+  uint32_t bID;        /* hash-block read (T), 1-based */
+  uint32_t flags;      /* bit 0: S reverse-complemented; bit 1: dropped by the filter */
+  uint32_t seeds;      /* k-mer seeds of the pair (diag_ct) */
+  uint32_t nodes;      /* match runs of the pair (its nodes in oic_get_pairs' node array) */
+  uint32_t overlaps;   /* records the DP emitted for the pair */
+  uint32_t cells;      /* DP cells spent on the pair (saturating) */
+  float    score;      /* filter logit (0 when no filter is set) */
+  uint32_t extensions; /* Extend_Alignment calls made for the pair */
+  int32_t  firstHit;   /* index of the first extension that added an overlap, -1 none */
+  uint32_t cellsFirst; /* DP cells of the pair's first extension */
+  uint32_t extLimit;   /* 1 when the filter's single-extension tier applied, else 0 */
+} oic_pair_info;
+
+/* Set the filter (params: host array of OIC_FILTER_NPARAM FP16 bit patterns) and its
+ * probability thresholds, p = sigmoid(logit):
+ *   p <  dropThreshold                  the pair is not extended;
+ *   dropThreshold <= p < fullThreshold  the pair stops after its first extension if
+ *                                       that extension found no overlap;
+ *   p >= fullThreshold                  every match is extended (the reference's rule).
+ * fullThreshold <= dropThreshold disables the middle tier.  params NULL turns the
+ * filter off. */
+int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float dropThreshold, float fullThreshold);
+
+/* Pair collection for training and evaluation: mode 0 off, 1 pairs and feature rows,
+ * 2 also the match runs (T offset, length, S start per run).  Collected data accumulate
+ * over runs until oic_clear_pairs(). */
+int oic_collect_pairs(oic_ctx *ctx, int mode);
+int oic_num_pairs(oic_ctx *ctx, uint64_t *nPairs, uint64_t *nNodes);
+/* Copies up to maxPairs pairs (info, and feat: OIC_FILTER_IN FP16 per pair, when
+ * non-NULL) and up to maxNodes runs (3 int32 each, when non-NULL), in collection order. */
+int oic_get_pairs(oic_ctx *ctx, oic_pair_info *info, uint16_t *feat, int32_t *nodes, uint64_t maxPairs,
+                  uint64_t maxNodes);
+int oic_clear_pairs(oic_ctx *ctx);
+
+/* Training and inference kernels of the filter network on caller-owned DEVICE
+ * buffers (stream: a cudaStream_t, NULL for the default stream; the calls return
+ * after launching).  X: n rows of OIC_FILTER_IN FP16.
+ *   oic_mlp_forward:  logit[n]; dH1/dH2 (n x 128 FP16 activations) when non-NULL.
+ *   oic_mlp_backward: adds to dGrad (OIC_FILTER_NPARAM FP32, parameter layout) the
+ *     gradient of sum_i weight_i * BCE(sigmoid(logit_i), label_i) (dWeight NULL: 1),
+ *     using dG1/dG2 (n x 128 FP16) as scratch; adds the loss to *dLoss when non-NULL.
+ *   oic_mlp_adam: one Adam step (bias-corrected, step >= 1, decoupled weight decay)
+ *     on FP32 master weights with gradient gradScale * dGrad; writes the FP16 copy
+ *     dParams and zeroes dGrad. */
+int oic_mlp_forward(const uint16_t *dParams, const uint16_t *dX, uint32_t n, float *dLogit, uint16_t *dH1,
+                    uint16_t *dH2, void *stream);
+int oic_mlp_backward(const uint16_t *dParams, const uint16_t *dX, const uint16_t *dH1, const uint16_t *dH2,
+                     const float *dLogit, const float *dLabel, const float *dWeight, uint32_t n, float *dGrad,
+                     uint16_t *dG1, uint16_t *dG2, float *dLoss, void *stream);
+int oic_mlp_adam(float *dMaster, float *dM, float *dV, float *dGrad, uint16_t *dParams, float lr, float beta1,
+                 float beta2, float eps, float gradScale, float weightDecay, uint32_t step, void *stream);
 
 /* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
  * min(n, table length) entries; *len gets the table length. */
