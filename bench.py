@@ -13,6 +13,10 @@ lists, and the banded edit-distance extensions that emit the overlap records.
   e2e    the same through the C ABI with host buffers: every step uploads the reads
          from pinned host memory, runs the job and copies the records back (wall clock).
 
+learned_filter  the same job with the learned candidate filter (weights trained on other
+         seeds of the c2 shape): overlaps/s, recall against this run's plain records,
+         and whether every filtered record equals its plain record.
+
 --impl reference times the CPU restatement of the reference (oracle/oic_port.c, the
 reference's algorithm step for step; canu's own sources cannot be built on the GPU
 host) on all host cores: the hash block is built once and timed, each step runs a
@@ -240,6 +244,7 @@ def main():
     ap.add_argument("--data-dir", default=os.environ.get("OIC_BENCH_DATA", "/tmp/oic_bench"))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-filter", action="store_true", help="skip the learned-filter leg")
     a = ap.parse_args()
     ws, rank, local = dist()
     cores = os.cpu_count() or 1
@@ -311,22 +316,55 @@ def main():
     ov.set_reads(lib_, ln, off, host_bases)
 
     peaks, peak_kind = measured_peaks()
-    clocks = Clocks(local)
-    res = []
-    for i in range(a.warmup + a.steps):
-        if i == a.warmup:
-            barrier_max(0.0, ws)
-            clocks.start()
-        t0 = time.perf_counter()
-        ov.clear()
-        ov.set_reads(lib_, ln, off, host_bases)        # H2D of the step's input (pinned)
-        ov.run()
-        rec = ov.overlaps()                            # D2H of the step's result
-        t1 = time.perf_counter()
-        st = ov.stats()
-        if i >= a.warmup:
-            res.append((st, t1 - t0, len(rec)))
-    clk = clocks.stop()
+
+    def timed(with_clocks):
+        """W untimed + K timed steps; each step uploads the reads, runs the job and reads
+        the records back.  Returns ([(stats, wall s, records)], clocks, last records)."""
+        clocks = Clocks(local) if with_clocks else None
+        out, rec = [], None
+        for i in range(a.warmup + a.steps):
+            if i == a.warmup:
+                barrier_max(0.0, ws)
+                if clocks:
+                    clocks.start()
+            t0 = time.perf_counter()
+            ov.clear()
+            ov.set_reads(lib_, ln, off, host_bases)        # H2D of the step's input (pinned)
+            ov.run()
+            rec = ov.overlaps()                            # D2H of the step's result
+            t1 = time.perf_counter()
+            st = ov.stats()
+            if i >= a.warmup:
+                out.append((st, t1 - t0, len(rec)))
+        return out, (clocks.stop() if clocks else None), rec
+
+    res, clk, plain_rec = timed(True)
+
+    # The learned candidate filter on the same reads (trained on other seeds).
+    filt = None
+    fpath = os.path.join(ROOT, "canu_gb300", "filter_c2.npz")
+    if a.workload == "c2" and os.path.exists(fpath) and not a.no_filter:
+        from canu_gb300 import filter_train
+        fprm, fthr, ffull, fmeta = filter_train.load(fpath)
+        ov.set_filter(fprm, fthr, ffull)
+        fres, _, frec = timed(False)
+        ov.set_filter(None, 0.0)
+        recall, exact = filter_train.compare(plain_rec, frec)
+        fms = statistics.mean(r[0]["msTotal"] for r in fres)
+        fe2e = statistics.mean(r[1] for r in fres)
+        fms_max, fe2e_max = barrier_max(fms, ws), barrier_max(fe2e, ws)
+        fst = fres[0][0]
+        filt = {"value": ws * fst["totalOverlaps"] / (fms_max / 1000.0), "unit": "overlaps/s",
+                "dp_cells_per_sec": ws * fst["dpCells"] / (fms_max / 1000.0),
+                "e2e": {"value": ws * fst["totalOverlaps"] / fe2e_max, "unit": "overlaps/s"},
+                "ms_per_step": fms_max, "overlaps_per_step": fst["totalOverlaps"],
+                "recall_vs_plain": recall, "records_identical_to_plain": exact,
+                "dp_cells": fst["dpCells"], "dp_cells_skipped_frac": None, "filtered_pairs": fst["filteredPairs"],
+                "ms_filter": fst["msFilter"], "ms_align": fst["msAlign"],
+                "thresholds": {"drop_below_p": fthr, "single_extension_below_p": ffull},
+                "trained_on": f"c2 seeds {fmeta.get('train_seeds')}; this read set is seed "
+                              f"{workloads.WORKLOADS[a.workload]['synth']['seed']} (held out)",
+                "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in fres))}
     ov.close()
 
     ms_dev = statistics.mean(r[0]["msTotal"] for r in res)
@@ -371,6 +409,10 @@ def main():
         "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in res)),
         "clocks": clk,
     }
+    if filt:
+        filt["dp_cells_skipped_frac"] = 1.0 - filt["dp_cells"] / max(cells, 1)
+        filt["speedup_vs_plain"] = filt["value"] / value
+        line["learned_filter"] = filt
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         cpu = CpuPath(a.workload, db, skip, cores)
         dt, ovs, nref, ccells, _ = cpu_sample(cpu, 1, a.cpu_seconds)

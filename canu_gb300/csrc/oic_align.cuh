@@ -143,6 +143,69 @@ static __device__ __noinline__ void set_left_delta(WarpDP &w, int e, int d, int 
   w.leftLen = n;
 }
 
+// Max_Score bookkeeping of forward()/reverse() (prefixEditDistance-forward.C:284-296,
+// -reverse.C:300-312), replayed once after the rows instead of on every row.  Row e
+// (1..eLast) stored its largest kept value in rowHdr[e].w.  Walking the rows in order,
+// the reference scores a row only when that value passes every earlier row's
+// (Longest grows) and keeps the first row whose score fl(fl(value * BMV) - e) is the
+// strict maximum above the initial 0.0.  Here lane i takes rows i+1, i+33, ...; a warp
+// max-scan finds the rows where Longest grows, each lane scores its rows in IEEE double
+// (the same two roundings), and a warp arg-max with the smallest row on ties picks the
+// reference's row.  msD is the first diagonal of that row's kept band holding msLen.
+static __device__ __noinline__ void max_score_rows(const WarpDP &w, int eLast, double &maxScore, int &msLen,
+                                                   int &msD, int &msE) {
+  const int    lane = threadIdx.x & 31;
+  const double BMV  = w.P.branchMatchValue;
+  double best  = 0.0;
+  int    bestE = INT_MAX;
+  int    carry = 0;   // Longest before the current block of 32 rows
+  for (int base = 1; base <= eLast; base += 32) {
+    const int e = base + lane;
+    const int v = e <= eLast ? w.sc.rowHdr[e].w : INT_MIN;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl = max(incl, t);
+    }
+    int excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) excl = INT_MIN;
+    if (e <= eLast && v > max(carry, excl)) {
+      const double s = __dsub_rn(__dmul_rn((double)v, BMV), (double)e);
+      if (s > best) {
+        best  = s;
+        bestE = e;
+      }
+    }
+    carry = max(carry, __shfl_sync(0xffffffffu, incl, 31));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int    oe = __shfl_xor_sync(0xffffffffu, bestE, o);
+    if (ob > best || (ob == best && oe < bestE)) {
+      best  = ob;
+      bestE = oe;
+    }
+  }
+  if (bestE == INT_MAX) {
+    maxScore = 0.0;
+    msLen = msD = msE = 0;
+    return;
+  }
+  maxScore     = best;
+  msE          = bestE;
+  const int4 h = w.sc.rowHdr[msE];
+  msLen        = h.w;
+  int myD = INT_MAX;
+  for (int d = h.y + lane; d <= h.z; d += 32)
+    if (w.sc.arena[h.x + d - h.y] == msLen) {
+      myD = d;
+      break;
+    }
+  msD = __reduce_min_sync(0xffffffffu, myD);
+}
+
 // forward() (prefixEditDistance-forward.C:94-314) for STEP = +1 and reverse()
 // (prefixEditDistance-reverse.C:114-330) for STEP = -1, cooperatively by one warp.
 // A[STEP*i] is base a0+STEP*i of view A, T likewise.  Returns the error count; the
@@ -177,7 +240,7 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
   __syncwarp();
 
   int    used = 1, prevBase = 0, L = 0, R = 0;
-  int    longest = 0, bestD = 0, bestE = 0, msLen = 0, msD = 0, msE = 0;
+  int    msLen = 0, msD = 0, msE = 0, eDone = 0;
   double maxScore = 0.0;
   int    e;
 
@@ -224,8 +287,9 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
     if (dEnd != INT_MAX) {
       w.cells += (unsigned long long)(dEnd - Lc + 1);
       const int row = cv[dEnd];
-      // Branch-point test in IEEE double on lane 0 (the FP64 pipe is narrow); lane 0
-      // holds maxScore, the other lanes take its decision.
+      max_score_rows(w, eDone, maxScore, msLen, msD, msE);
+      // Branch-point test in IEEE double on lane 0 (the FP64 pipe is narrow); the
+      // other lanes take its decision.
       int abort_ = 0;
       if (lane == 0) {
         const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
@@ -280,40 +344,20 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
     if (L2 == INT_MAX) break;
     const int R2 = __reduce_max_sync(0xffffffffu, myR);
 
-    // Longest row on the kept band, first diagonal on ties (forward.C:284-289).
-    int myV = -1, myD = INT_MAX;
-    for (int d = L2 + lane; d <= R2; d += 32) {
-      const int v = cv[d];
-      if (v > myV) { myV = v; myD = d; }
-    }
+    // Largest value on the kept band (forward.C:284-289); the Max_Score test that uses
+    // it runs once after the rows (max_score_rows).  Score only moves when Longest
+    // does: with Longest unchanged, rounding is monotone, so Longest*BMV - e cannot pass
+    // the Max_Score of an earlier row.
+    int myV = -1;
+    for (int d = L2 + lane; d <= R2; d += 32) myV = max(myV, cv[d]);
     const int rowMax = __reduce_max_sync(0xffffffffu, myV);
-    if (rowMax > longest) {
-      longest = rowMax;
-      bestD   = __reduce_min_sync(0xffffffffu, myV == rowMax ? myD : INT_MAX);
-      bestE   = e;
-      // Score only moves up when Longest does: with Longest unchanged, rounding is
-      // monotone, so Longest*BMV - e cannot pass the Max_Score of an earlier row.
-      int u = 0;
-      if (lane == 0) {
-        const double score = __dsub_rn(__dmul_rn((double)longest, BMV), (double)e);
-        if (score > maxScore) {
-          maxScore = score;
-          u        = 1;
-        }
-      }
-      const bool upd = __shfl_sync(0xffffffffu, u, 0) != 0;
-      if (upd) {
-        msLen = longest;
-        msD   = bestD;
-        msE   = bestE;
-      }
-    }
 
     // Keep the band for the traceback.
     const int cnt = R2 - L2 + 1;
     if (used + cnt > w.cap.arenaCap) { w.err |= kErrArenaFull; return 0; }
     for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cv[d];
-    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, 0);
+    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
+    eDone = e;
     used += cnt;
     int *t = prev;
     prev   = cur;
@@ -325,6 +369,8 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
   }
 
   // Errors exhausted or every diagonal pruned (forward.C:306-313).
+  __syncwarp();
+  max_score_rows(w, eDone, maxScore, msLen, msD, msE);
   aEnd = STEP * msLen;
   tEnd = STEP * (msLen + msD);
   __syncwarp();
