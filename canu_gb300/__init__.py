@@ -29,7 +29,8 @@ EXPORTS = (
     "oic_load_hash_block", "oic_run_refs", "oic_run", "oic_num_overlaps", "oic_fetch_overlaps",
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
     "oic_extend_batch_noalloc", "oic_set_filter", "oic_collect_pairs", "oic_num_pairs", "oic_get_pairs",
-    "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam",
+    "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam", "oic_set_tuning", "oic_get_tuning",
+    "oic_autotune",
 )
 
 # Learned candidate filter (include/oic_gpu.h): feature row width, hidden width and the
@@ -76,10 +77,22 @@ class OicStats(ctypes.Structure):
         ("msHash", ctypes.c_double), ("msSeed", ctypes.c_double),
         ("msAlign", ctypes.c_double), ("msTotal", ctypes.c_double),
         ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64), ("dpCellsNoOverlap", ctypes.c_uint64),
-        ("filteredPairs", ctypes.c_uint64), ("msFilter", ctypes.c_double)]
+        ("filteredPairs", ctypes.c_uint64), ("msFilter", ctypes.c_double),
+        ("msNarrow", ctypes.c_double), ("msWide", ctypes.c_double), ("pairsNarrow", ctypes.c_uint64),
+        ("pairsWide", ctypes.c_uint64), ("cellsWide", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class OicTuning(ctypes.Structure):
+    """oic_tuning: DP launch configuration (zeros = defaults)."""
+    _fields_ = [("narrowArena", ctypes.c_uint32), ("wideMinLen", ctypes.c_uint32), ("wideThreads", ctypes.c_uint32),
+                ("wideTile", ctypes.c_uint32), ("wideBandW", ctypes.c_uint32), ("wideCtas", ctypes.c_uint32),
+                ("wideArena", ctypes.c_uint64), ("forceWide", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
 
 
 _lib = None
@@ -118,6 +131,9 @@ def library():
         lib.oic_mlp_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, U32, vp, vp, vp, vp, vp]
         F = ctypes.c_float
         lib.oic_mlp_adam.argtypes = [vp, vp, vp, vp, vp, F, F, F, F, F, F, U32, vp]
+        lib.oic_set_tuning.argtypes = [vp, P(OicTuning)]
+        lib.oic_get_tuning.argtypes = [vp, P(OicTuning)]
+        lib.oic_autotune.argtypes = [vp, U32, U32, vp, U32, P(U32)]
         lib.oic_last_error.argtypes = [vp]
         lib.oic_last_error.restype = ctypes.c_char_p
         _lib = lib
@@ -280,6 +296,30 @@ class Overlapper:
 
     def clear_pairs(self):
         self._check(self._lib.oic_clear_pairs(self._ctx))
+
+    def set_tuning(self, **kw):
+        """DP launch configuration by field name (OicTuning); no arguments: defaults."""
+        if not kw:
+            self._check(self._lib.oic_set_tuning(self._ctx, None))
+            return
+        t = OicTuning()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self._lib.oic_set_tuning(self._ctx, ctypes.byref(t)))
+
+    def tuning(self):
+        t = OicTuning()
+        self._check(self._lib.oic_get_tuning(self._ctx, ctypes.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, bgn, end, max_lines=64):
+        """Time the DP grid on ref reads [bgn, end] of the loaded block; sets the fastest.
+        Returns one dict per configuration."""
+        rep = np.zeros((max_lines, 8), dtype=np.float64)
+        n = ctypes.c_uint32()
+        self._check(self._lib.oic_autotune(self._ctx, bgn, end, _ptr(rep), max_lines, ctypes.byref(n)))
+        keys = ("wideTile", "wideThreads", "wideMinLen", "msNarrow", "msWide", "msTotal", "pairsNarrow", "cellsWide")
+        return [dict(zip(keys, map(float, r))) for r in rep[: n.value]]
 
     def extend_batch(self, sRead, sRev, tRead, mStart, mOffset, mLen):
         """Batched Extend_Alignment; returns (out[n,5], kind[n], deltaLen[n])."""

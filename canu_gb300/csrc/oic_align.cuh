@@ -43,6 +43,9 @@ struct WarpDP {
   unsigned long long cells, slides, rows;
   u32                err;           // capacity error of the current pair (0 = ok)
   int                leftLen, rightLen;
+  struct GroupShared *gs;           // non-null: warp 0 of a group CTA (row loops on all warps)
+  int                gThreads;      // threads of the group CTA
+  int                gU;            // diagonals per thread per pass in the group row loop
 };
 
 // The scratch of global warp gw inside the base allocations of a configuration.
@@ -206,51 +209,67 @@ static __device__ __noinline__ void max_score_rows(const WarpDP &w, int eLast, d
   msD = __reduce_min_sync(0xffffffffu, myD);
 }
 
-// forward() (prefixEditDistance-forward.C:94-314) for STEP = +1 and reverse()
-// (prefixEditDistance-reverse.C:114-330) for STEP = -1, cooperatively by one warp.
-// A[STEP*i] is base a0+STEP*i of view A, T likewise.  Returns the error count; the
-// outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
+// ---------------------------------------------------------------------------------
+// Row loop of forward()/reverse() (prefixEditDistance-forward.C:131-304,
+// -reverse.C:151-320): error rows e = 1, 2, ... with the band pruned against
+// Edit_Match_Limit.  It stops at the first row where a diagonal reaches the end of A
+// or T (kRowsEnd), when every diagonal is pruned or the error limit is reached
+// (kRowsDone), or on a capacity limit (kRowsErr).  Every kept row goes to the arena
+// with its largest value in the row header (see max_score_rows).
+enum { kRowsDone = 0, kRowsEnd = 1, kRowsErr = 2 };
+
+struct RowsOut {
+  int  status;
+  u32  err;
+  int  e, dEnd, eDone;       // end row, first diagonal reaching an end, last kept row
+  int  Lc, Rc, prevBase;     // band of row e and the base of row e-1
+  int *prev, *cur;           // row e-1 and row e buffers
+  unsigned long long cells, rows;
+};
+
+// Several warps of one CTA on one pair (the wide bins): warp 0 runs the pair logic and
+// hands each extension's row loop to the whole CTA through GroupShared.
+struct GroupJob {
+  SeqView A, T;
+  i64     a0, t0;
+  int     m, n, errorLimit, step, u;
+  int    *rowA, *rowB;       // row buffers (rowA holds row 0)
+};
+struct GroupShared {
+  GroupJob job;
+  int      cmd;              // kGroupRows or kGroupExit, posted by warp 0 before barrier 1
+  int      red[32][4];       // per-warp partial reductions of a row
+};
+enum { kGroupRows = 1, kGroupExit = 2 };
+
+// Named barrier over the CTA's nThr threads (id 1: hand-off, id 2: rows).
+__device__ __forceinline__ void group_bar(int id, int nThr) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nThr) : "memory");
+}
+
+// The row loop by one warp.  Row 0 (value r0) is in prev[2].
 template <int STEP>
-static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
-                              int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
+__device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0,
+                                             int n, int errorLimit) {
   const int lane = threadIdx.x & 31;
-  const double BMV = w.P.branchMatchValue;
-
-  if (STEP > 0) w.rightLen = 0;
-  else w.leftLen = 0;
-
-  const int r0 = warp_slide0<STEP>(A, a0, T, t0, m, w.slides);
-  if (r0 == m) {
-    aEnd = tEnd = STEP * m;
-    if (STEP < 0) leftover = m;
-    toEnd = true;
-    return 0;
-  }
-
-  if (lane == 0) {
-    w.sc.arena[0]  = r0;
-    w.sc.rowHdr[0] = make_int4(0, 0, 0, 0);
-  }
+  RowsOut o;
+  o.status = kRowsDone;
+  o.err = 0;
+  o.e = o.dEnd = o.eDone = 0;
+  o.cells = o.rows = 0;
   // Row buffers hold diagonal d at index d - base + 2.  Before a row is computed the
   // two diagonals on each side of the previous row's kept band are set to -2, as the
   // reference does (forward.C:150-153), so the neighbour reads need no bounds tests.
   int *prev = w.smA, *cur = w.smB;
   int  bufW = w.cap.bandW;
-  if (lane == 0) prev[2] = r0;
-  __syncwarp();
-
-  int    used = 1, prevBase = 0, L = 0, R = 0;
-  int    msLen = 0, msD = 0, msE = 0, eDone = 0;
-  double maxScore = 0.0;
-  int    e;
-
-  for (e = 1; e <= errorLimit; e++) {
-    if (e >= w.cap.rowCap) { w.err |= kErrRowsFull; return 0; }
+  int  used = 1, prevBase = 0, L = 0, R = 0;
+  for (int e = 1; e <= errorLimit; e++) {
+    if (e >= w.cap.rowCap) { o.status = kRowsErr; o.err = kErrRowsFull; break; }
     const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
     const int width = Rc - Lc + 1;
     if (width + 4 > bufW) {
       // The band outgrew the shared-memory rows: continue in the warp's HBM rows.
-      if (bufW == w.cap.rowsGW || width + 4 > w.cap.rowsGW || !w.sc.rowsG) { w.err |= kErrBandWide; return 0; }
+      if (bufW == w.cap.rowsGW || width + 4 > w.cap.rowsGW || !w.sc.rowsG) { o.status = kRowsErr; o.err = kErrBandWide; break; }
       int *gA = w.sc.rowsG, *gB = w.sc.rowsG + w.cap.rowsGW;
       for (int i = lane; i < bufW; i += 32) gA[i] = prev[i];
       __syncwarp();
@@ -281,46 +300,288 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
       }
     }
     __syncwarp();
-    w.rows++;
+    o.rows++;
     const int dEnd = __reduce_min_sync(0xffffffffu, myEnd);
-
     if (dEnd != INT_MAX) {
-      w.cells += (unsigned long long)(dEnd - Lc + 1);
-      const int row = cv[dEnd];
-      max_score_rows(w, eDone, maxScore, msLen, msD, msE);
-      // Branch-point test in IEEE double on lane 0 (the FP64 pipe is narrow); the
-      // other lanes take its decision.
-      int abort_ = 0;
+      o.cells += (unsigned long long)(dEnd - Lc + 1);
+      o.status   = kRowsEnd;
+      o.e        = e;
+      o.dEnd     = dEnd;
+      o.Lc       = Lc;
+      o.Rc       = Rc;
+      o.prevBase = prevBase;
+      o.prev     = prev;
+      o.cur      = cur;
+      break;
+    }
+    o.cells += (unsigned long long)width;
+
+    // The kept band is [first, last] unpruned diagonal (forward.C:245-280).
+    const int L2 = __reduce_min_sync(0xffffffffu, myL);
+    if (L2 == INT_MAX) break;
+    const int R2 = __reduce_max_sync(0xffffffffu, myR);
+
+    // Largest value on the kept band (forward.C:284-289); the Max_Score test that uses
+    // it runs once after the rows (max_score_rows).
+    int myV = -1;
+    for (int d = L2 + lane; d <= R2; d += 32) myV = max(myV, cv[d]);
+    const int rowMax = __reduce_max_sync(0xffffffffu, myV);
+
+    // Keep the band for the traceback.
+    const int cnt = R2 - L2 + 1;
+    if (used + cnt > w.cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
+    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cv[d];
+    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
+    used += cnt;
+    int *t = prev;
+    prev   = cur;
+    cur    = t;
+    prevBase = Lc;
+    L        = L2;
+    R        = R2;
+    o.eDone  = e;
+    __syncwarp();
+  }
+  return o;
+}
+
+// The row loop by every thread of the CTA (nThr threads, tid = threadIdx.x).  Thread t
+// takes U consecutive diagonals per pass, d0 = Lc + U*t + U*nThr*k, so the U+2
+// neighbour values of row e-1 are read once for U cells and U slides are in flight.
+// Every decision is made on CTA-reduced values, so all threads take the same path and
+// meet the same barriers.
+template <int STEP, int U>
+static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpScratch &sc, const AlignCaps &cap,
+                                                  const int *eml, int tid, int nThr, int (*red)[4],
+                                                  unsigned long long &slides) {
+  const int lane = tid & 31, wid = tid >> 5, nW = nThr >> 5;
+  RowsOut o;
+  o.status = kRowsDone;
+  o.err = 0;
+  o.e = o.dEnd = o.eDone = 0;
+  o.cells = o.rows = 0;
+  // Every thread has read the job before warp 0 can post the next one.
+  group_bar(2, nThr);
+  int *prev = j.rowA, *cur = j.rowB;
+  int  bufW = cap.bandW;
+  int  used = 1, prevBase = 0, L = 0, R = 0;
+  for (int e = 1; e <= j.errorLimit; e++) {
+    if (e >= cap.rowCap) { o.status = kRowsErr; o.err = kErrRowsFull; break; }
+    const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
+    const int width = Rc - Lc + 1;
+    if (width + 4 > bufW) {
+      if (bufW == cap.rowsGW || width + 4 > cap.rowsGW || !sc.rowsG) { o.status = kRowsErr; o.err = kErrBandWide; break; }
+      int *gA = sc.rowsG, *gB = sc.rowsG + cap.rowsGW;
+      for (int i = tid; i < bufW; i += nThr) gA[i] = prev[i];
+      group_bar(2, nThr);
+      prev = gA;
+      cur  = gB;
+      bufW = cap.rowsGW;
+    }
+    const int lim = eml[e];
+    if (tid < 4) prev[(tid < 2 ? L - 2 + tid : R - 1 + tid) - prevBase + 2] = -2;
+    group_bar(2, nThr);
+    const int *pv = prev + (2 - prevBase);
+    int       *cv = cur + (2 - Lc);
+    int myEnd = INT_MAX, myL = INT_MAX, myR = INT_MIN;
+    for (int d0 = Lc + tid * U; d0 <= Rc; d0 += nThr * U) {
+      int q[U + 2];   // row e-1 at d0-1 .. d0+U
+#pragma unroll
+      for (int k = 0; k < U + 2; k++) q[k] = (d0 - 1 + k <= Rc + 1) ? pv[d0 - 1 + k] : -2;
+#pragma unroll
+      for (int k = 0; k < U; k++) {
+        const int d = d0 + k;
+        if (d <= Rc) {
+          int row = 1 + q[k + 1];
+          if (q[k] > row) row = q[k];
+          if (1 + q[k + 2] > row) row = 1 + q[k + 2];
+          const int room = min(j.m - row, j.n - row - d);
+          if (room > 0) row += slide<STEP>(j.A, j.a0, j.T, j.t0, row, d, room, slides);
+          cv[d] = row;
+          if ((row == j.m || row + d == j.n) && d < myEnd) myEnd = d;
+          if (!(row + max(d, 0) < lim)) {
+            if (myL == INT_MAX) myL = d;
+            myR = d;
+          }
+        }
+      }
+    }
+    {
+      const int wEnd = __reduce_min_sync(0xffffffffu, myEnd);
+      const int wL   = __reduce_min_sync(0xffffffffu, myL);
+      const int wR   = __reduce_max_sync(0xffffffffu, myR);
       if (lane == 0) {
-        const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
-        const int    tailLen = row - msLen;
-        const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
-        abort_ = (w.P.partial && score < maxScore) ||
-                 (e > 20 / 2 && tailLen >= 20 && slope >= w.P.minBranchTailSlope);
+        red[wid][0] = wEnd;
+        red[wid][1] = wL;
+        red[wid][2] = wR;
       }
-      abort_ = __shfl_sync(0xffffffffu, abort_, 0);
-      if (abort_) {
-        aEnd = STEP * msLen;
-        tEnd = STEP * (msLen + msD);
-        if (lane == 0) {
-          const int last = arena_get(w, msE, msD);
-          if (STEP > 0) set_right_delta(w, msE, msD, last);
-          else set_left_delta(w, msE, msD, last, leftover, tEnd, n);
-        }
-        if (STEP > 0) w.rightLen = __shfl_sync(0xffffffffu, w.rightLen, 0);
-        else {
-          w.leftLen = __shfl_sync(0xffffffffu, w.leftLen, 0);
-          leftover  = __shfl_sync(0xffffffffu, leftover, 0);
-          tEnd      = __shfl_sync(0xffffffffu, tEnd, 0);
-        }
-        toEnd = false;
-        __syncwarp();
-        return msE;
+    }
+    group_bar(2, nThr);
+    int dEnd = INT_MAX, L2 = INT_MAX, R2 = INT_MIN;
+    for (int i = 0; i < nW; i++) {
+      dEnd = min(dEnd, red[i][0]);
+      L2   = min(L2, red[i][1]);
+      R2   = max(R2, red[i][2]);
+    }
+    o.rows++;
+    if (dEnd != INT_MAX) {
+      o.cells += (unsigned long long)(dEnd - Lc + 1);
+      o.status   = kRowsEnd;
+      o.e        = e;
+      o.dEnd     = dEnd;
+      o.Lc       = Lc;
+      o.Rc       = Rc;
+      o.prevBase = prevBase;
+      o.prev     = prev;
+      o.cur      = cur;
+      break;
+    }
+    o.cells += (unsigned long long)width;
+    if (L2 == INT_MAX) break;
+
+    int myV = -1;
+    for (int d0 = Lc + tid * U; d0 <= Rc; d0 += nThr * U)
+#pragma unroll
+      for (int k = 0; k < U; k++) {
+        const int d = d0 + k;
+        if (d >= L2 && d <= R2) myV = max(myV, cv[d]);
       }
-      int d = dEnd;
+    {
+      const int wV = __reduce_max_sync(0xffffffffu, myV);
+      if (lane == 0) red[wid][3] = wV;
+    }
+    group_bar(2, nThr);
+    int rowMax = -1;
+    for (int i = 0; i < nW; i++) rowMax = max(rowMax, red[i][3]);
+
+    const int cnt = R2 - L2 + 1;
+    if (used + cnt > cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
+    for (int d = L2 + tid; d <= R2; d += nThr) sc.arena[used + d - L2] = cv[d];
+    if (tid == 0) sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
+    used += cnt;
+    int *t = prev;
+    prev   = cur;
+    cur    = t;
+    prevBase = Lc;
+    L        = L2;
+    R        = R2;
+    o.eDone  = e;
+    group_bar(2, nThr);
+  }
+  return o;
+}
+
+// The job a GroupJob names, with its compile-time step and tile.
+static __device__ __forceinline__ RowsOut group_rows_any(const GroupJob &j, const WarpScratch &sc,
+                                                         const AlignCaps &cap, const int *eml, int tid, int nThr,
+                                                         int (*red)[4], unsigned long long &slides) {
+  if (j.step > 0) {
+    if (j.u == 4) return group_rows<+1, 4>(j, sc, cap, eml, tid, nThr, red, slides);
+    if (j.u == 2) return group_rows<+1, 2>(j, sc, cap, eml, tid, nThr, red, slides);
+    return group_rows<+1, 1>(j, sc, cap, eml, tid, nThr, red, slides);
+  }
+  if (j.u == 4) return group_rows<-1, 4>(j, sc, cap, eml, tid, nThr, red, slides);
+  if (j.u == 2) return group_rows<-1, 2>(j, sc, cap, eml, tid, nThr, red, slides);
+  return group_rows<-1, 1>(j, sc, cap, eml, tid, nThr, red, slides);
+}
+
+// Worker warps of a group CTA: run the row loops warp 0 posts until it posts exit.
+static __device__ __noinline__ void group_worker(GroupShared &gs, const WarpScratch &sc, const AlignCaps &cap,
+                                                 const int *eml, unsigned long long &slides) {
+  const int tid = threadIdx.x, nThr = blockDim.x;
+  while (true) {
+    group_bar(1, nThr);
+    if (gs.cmd != kGroupRows) break;
+    const GroupJob j = gs.job;
+    group_rows_any(j, sc, cap, eml, tid, nThr, gs.red, slides);
+  }
+}
+
+// forward() (prefixEditDistance-forward.C:94-314) for STEP = +1 and reverse()
+// (prefixEditDistance-reverse.C:114-330) for STEP = -1.  A[STEP*i] is base a0+STEP*i of
+// view A, T likewise.  The row loop runs on this warp, or on the whole CTA when w.gs is
+// set (warp 0 of a group CTA); the rest runs on this warp.  Returns the error count;
+// the outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
+template <int STEP, bool GROUP>
+static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
+                              int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
+  const int lane = threadIdx.x & 31;
+  const double BMV = w.P.branchMatchValue;
+
+  if (STEP > 0) w.rightLen = 0;
+  else w.leftLen = 0;
+
+  const int r0 = warp_slide0<STEP>(A, a0, T, t0, m, w.slides);
+  if (r0 == m) {
+    aEnd = tEnd = STEP * m;
+    if (STEP < 0) leftover = m;
+    toEnd = true;
+    return 0;
+  }
+
+  if (lane == 0) {
+    w.sc.arena[0]  = r0;
+    w.sc.rowHdr[0] = make_int4(0, 0, 0, 0);
+    w.smA[2]       = r0;
+  }
+  __syncwarp();
+
+  RowsOut o;
+  if (GROUP) {
+    if (lane == 0) {
+      GroupJob &j  = w.gs->job;
+      j.A          = A;
+      j.T          = T;
+      j.a0         = a0;
+      j.t0         = t0;
+      j.m          = m;
+      j.n          = n;
+      j.errorLimit = errorLimit;
+      j.step       = STEP;
+      j.u          = w.gU;
+      j.rowA       = w.smA;
+      j.rowB       = w.smB;
+      w.gs->cmd    = kGroupRows;
+    }
+    __syncwarp();
+    group_bar(1, w.gThreads);
+    const GroupJob j = w.gs->job;
+    o = group_rows_any(j, w.sc, w.cap, w.eml, lane, w.gThreads, w.gs->red, w.slides);
+  } else {
+    o = warp_rows<STEP>(w, A, a0, m, T, t0, n, errorLimit);
+  }
+  w.cells += o.cells;
+  w.rows += o.rows;
+  if (o.status == kRowsErr) {
+    w.err |= o.err;
+    return 0;
+  }
+
+  double maxScore = 0.0;
+  int    msLen = 0, msD = 0, msE = 0;
+  max_score_rows(w, o.eDone, maxScore, msLen, msD, msE);
+
+  if (o.status == kRowsEnd) {
+    const int  e   = o.e;
+    const int *pv  = o.prev + (2 - o.prevBase);
+    const int *cv  = o.cur + (2 - o.Lc);
+    const int  row = cv[o.dEnd];
+    // Branch-point test in IEEE double on lane 0 (the FP64 pipe is narrow); the other
+    // lanes take its decision.
+    int abort_ = 0;
+    if (lane == 0) {
+      const double score   = __dsub_rn(__dmul_rn((double)row, BMV), (double)e);
+      const int    tailLen = row - msLen;
+      const double slope   = __ddiv_rn(__dsub_rn(maxScore, score), (double)tailLen);
+      abort_ = (w.P.partial && score < maxScore) ||
+               (e > 20 / 2 && tailLen >= 20 && slope >= w.P.minBranchTailSlope);
+    }
+    abort_ = __shfl_sync(0xffffffffu, abort_, 0);
+    if (!abort_) {
+      int d = o.dEnd;
       if (STEP > 0) {
         // Force the last error to be a mismatch (forward.C:215-221).
-        if (row == m && 1 + pv[d + 1] == row && d < Rc) d++;
+        if (row == m && 1 + pv[d + 1] == row && d < o.Rc) d++;
         aEnd = row;
         tEnd = row + d;
         if (lane == 0) set_right_delta(w, e, d, row);
@@ -337,40 +598,10 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
       __syncwarp();
       return e;
     }
-    w.cells += (unsigned long long)width;
-
-    // The kept band is [first, last] unpruned diagonal (forward.C:245-280).
-    const int L2 = __reduce_min_sync(0xffffffffu, myL);
-    if (L2 == INT_MAX) break;
-    const int R2 = __reduce_max_sync(0xffffffffu, myR);
-
-    // Largest value on the kept band (forward.C:284-289); the Max_Score test that uses
-    // it runs once after the rows (max_score_rows).  Score only moves when Longest
-    // does: with Longest unchanged, rounding is monotone, so Longest*BMV - e cannot pass
-    // the Max_Score of an earlier row.
-    int myV = -1;
-    for (int d = L2 + lane; d <= R2; d += 32) myV = max(myV, cv[d]);
-    const int rowMax = __reduce_max_sync(0xffffffffu, myV);
-
-    // Keep the band for the traceback.
-    const int cnt = R2 - L2 + 1;
-    if (used + cnt > w.cap.arenaCap) { w.err |= kErrArenaFull; return 0; }
-    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cv[d];
-    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
-    eDone = e;
-    used += cnt;
-    int *t = prev;
-    prev   = cur;
-    cur    = t;
-    prevBase = Lc;
-    L        = L2;
-    R        = R2;
-    __syncwarp();
   }
 
-  // Errors exhausted or every diagonal pruned (forward.C:306-313).
-  __syncwarp();
-  max_score_rows(w, eDone, maxScore, msLen, msD, msE);
+  // Branch point, errors exhausted, or every diagonal pruned (forward.C:197-212,
+  // 306-313): the alignment ends at the Max_Score row.
   aEnd = STEP * msLen;
   tEnd = STEP * (msLen + msD);
   __syncwarp();
@@ -390,10 +621,29 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
   return msE;
 }
 
+static __device__ __forceinline__ void warp_dp_init(WarpDP &w, const WarpScratch &sc, const AlignCaps &cap, int *smA,
+                                                    int *smB, const int *eml, const DevParams &P) {
+  w.sc       = sc;
+  w.cap      = cap;
+  w.smA      = smA;
+  w.smB      = smB;
+  w.eml      = eml;
+  w.P        = P;
+  w.cells    = 0;
+  w.slides   = 0;
+  w.rows     = 0;
+  w.err      = 0;
+  w.leftLen  = w.rightLen = 0;
+  w.gs       = nullptr;
+  w.gThreads = 32;
+  w.gU       = 1;
+}
+
 enum { kNone = 0, kLeftBranch = 1, kRightBranch = 2, kDovetail = 3 };
 
 // Extend_Alignment (prefixEditDistance-extend.C:36-183), one warp.  The merged delta
 // ends up in sc.deltaL[0 .. leftLen).  Outputs are warp-uniform.
+template <bool GROUP>
 static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int sLen, const SeqView &T, int tLen, int mStart,
                            int mOffset, int mLen, int &sLo, int &sHi, int &tLo, int &tHi, int &errors) {
   const int lane = threadIdx.x & 31;
@@ -412,12 +662,12 @@ static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int 
     sHi = tHi = 0;
     rToEnd    = true;
   } else if (sRightLen <= tRightLen) {
-    rightErrors = warp_prefix_dp<+1>(w, S, sRightBegin, sRightLen, T, tRightBegin, tRightLen, errorLimit, sHi, tHi,
+    rightErrors = warp_prefix_dp<+1, GROUP>(w, S, sRightBegin, sRightLen, T, tRightBegin, tRightLen, errorLimit, sHi, tHi,
                                      leftover, rToEnd);
     if (w.err) return kNone;
     for (int i = lane; i < w.rightLen; i += 32) w.sc.deltaR[i] = -w.sc.deltaR[i];
   } else {
-    rightErrors = warp_prefix_dp<+1>(w, T, tRightBegin, tRightLen, S, sRightBegin, sRightLen, errorLimit, tHi, sHi,
+    rightErrors = warp_prefix_dp<+1, GROUP>(w, T, tRightBegin, tRightLen, S, sRightBegin, sRightLen, errorLimit, tHi, sHi,
                                      leftover, rToEnd);
     if (w.err) return kNone;
   }
@@ -430,11 +680,11 @@ static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int 
     sLo = tLo = 0;
     lToEnd    = true;
   } else if (sRightBegin <= tRightBegin) {
-    leftErrors = warp_prefix_dp<-1>(w, S, sLeftBegin, sLeftBegin + 1, T, tLeftBegin, tLeftBegin + 1,
+    leftErrors = warp_prefix_dp<-1, GROUP>(w, S, sLeftBegin, sLeftBegin + 1, T, tLeftBegin, tLeftBegin + 1,
                                     errorLimit - rightErrors, sLo, tLo, leftover, lToEnd);
     if (w.err) return kNone;
   } else {
-    leftErrors = warp_prefix_dp<-1>(w, T, tLeftBegin, tLeftBegin + 1, S, sLeftBegin, sLeftBegin + 1,
+    leftErrors = warp_prefix_dp<-1, GROUP>(w, T, tLeftBegin, tLeftBegin + 1, S, sLeftBegin, sLeftBegin + 1,
                                     errorLimit - rightErrors, tLo, sLo, leftover, lToEnd);
     if (w.err) return kNone;
     for (int i = lane; i < w.leftLen; i += 32) w.sc.deltaL[i] = -w.sc.deltaL[i];

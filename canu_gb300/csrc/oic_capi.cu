@@ -161,6 +161,8 @@ struct oic_ctx {
   std::vector<uint16_t>      colFeat;
   std::vector<int32_t>       colNodes;
 
+  oic_tuning tune{};            // DP launch configuration (zeros: defaults)
+
   std::vector<uint32_t> out;   // accumulated records, 6 words each
   oic_stats stats{};
 };
@@ -263,18 +265,6 @@ AlignConfig align_normal(const oic_ctx *c) {
   a.caps.rowsGW   = 16384;
   return a;
 }
-AlignConfig align_wide(const oic_ctx *c) {
-  AlignConfig a;
-  a.bandW         = 8192;
-  a.warps         = c->nSM;
-  a.caps.arenaCap = 1 << 24;
-  a.caps.rowCap   = 1 << 18;
-  a.caps.nodeCap  = 1 << 22;
-  a.caps.bandW    = 8192;
-  a.caps.rowsGW   = 1 << 17;
-  return a;
-}
-
 int ensure_align_scratch(oic_ctx *ctx, const AlignConfig &ac, bool wide, WarpScratch &s) {
   const size_t W = (size_t)ac.warps;
   DevBuf &ar = wide ? ctx->dArena2 : ctx->dArena;
@@ -360,16 +350,62 @@ int collect_batch(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, bool filtered)
   return OIC_OK;
 }
 
-// Process one batch of eligible ref reads against the loaded block.  Returns OIC_OK,
-// or OIC_ERR_OVERFLOW when the batch's output did not fit (caller splits the batch).
-int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
-              cudaEvent_t evAln1, float &msSeed, float &msAlign) {
+uint32_t resolved_tuning_ctas(const oic_ctx *c, const oic_tuning &t);
+
+// The DP launch configuration with defaults filled in (include/oic_gpu.h).
+oic_tuning resolved_tuning(const oic_ctx *c) {
+  oic_tuning t = c->tune;
+  if (!t.narrowArena) t.narrowArena = 1u << 20;
+  if (!t.wideMinLen) t.wideMinLen = 0xffffffffu;
+  if (t.forceWide) t.wideMinLen = 0;
+  if (!t.wideThreads) t.wideThreads = 256;
+  if (!t.wideTile) t.wideTile = 1;
+  if (!t.wideBandW) t.wideBandW = 12288;
+  if (!t.wideCtas) t.wideCtas = resolved_tuning_ctas(c, t);
+  return t;
+}
+
+// The CTA bin's scratch: `ctas` CTAs, each with an arena of `arena` kept cells (0: a
+// share of the free memory).  `huge` is the last-resort rerun: 8 CTAs splitting most of
+// the free memory, HBM rows up to 2^20 diagonals.
+int ensure_group_scratch(oic_ctx *ctx, const oic_tuning &t, bool huge, uint32_t &ctas, AlignCaps &caps,
+                         WarpScratch &ws) {
+  caps.rowCap  = 1 << 18;
+  caps.nodeCap = 1 << 22;
+  caps.bandW   = (int)t.wideBandW;
+  caps.rowsGW  = huge ? 1 << 20 : 1 << 18;
+  ctas         = huge ? 8u : t.wideCtas;
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  freeB += ctx->dArena2.cap;   // released before the arena is reallocated
+  const size_t fixedPer = (size_t)caps.rowCap * (16 + 12) + (size_t)caps.rowsGW * 8 + caps.nodeCap + 64;
+  uint64_t cells = huge ? 0 : t.wideArena;
+  if (!cells) {
+    const double share = huge ? 0.7 : 0.4;
+    double per = share * (double)freeB / ctas - (double)fixedPer;
+    cells      = per > 0 ? (uint64_t)(per / sizeof(int)) : 0;
+    cells      = std::min<uint64_t>(cells, huge ? 0x7fff0000ull : (1ull << 24));
+  }
+  if (cells < (1u << 20)) return fail(ctx, OIC_ERR_NOMEM, "not enough device memory for the CTA-bin DP arena");
+  caps.arenaCap = (int)std::min<uint64_t>(cells, 0x7fff0000ull);
+  AlignConfig ac;
+  ac.bandW = caps.bandW;
+  ac.warps = (int)ctas;
+  ac.caps  = caps;
+  if (ctx->dArena2.cap < (size_t)ctas * caps.arenaCap * sizeof(int)) ctx->dArena2.release();
+  return ensure_align_scratch(ctx, ac, true, ws);
+}
+
+// Seed stage of a batch: the ref reads' seeds replayed into candidate pairs and match
+// runs (dPairs, dNodes), then their filter scores when a filter is set or pairs are
+// collected.  Returns OIC_OK, kRetrySmaller when the batch's output did not fit.
+int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
+               uint32_t &nPairs, uint32_t &nNodes) {
   const uint32_t nSeg = nRefs * 2;
   CK(ctx->dSegReads.ensure((size_t)nRefs * sizeof(uint32_t)));
   CK(cudaMemcpyAsync(ctx->dSegReads.p, refs, (size_t)nRefs * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemsetAsync(ctx->dCtr.p, 0, 64 * sizeof(uint32_t) + 0, ctx->st));
   CK(cudaMemsetAsync(ctr64(ctx) + kSeedStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
-  CK(cudaMemsetAsync(ctr64(ctx) + kAlignStatBase, 0, kStCount * sizeof(unsigned long long), ctx->st));
   CK(ctx->dSegOvf.ensure((size_t)nSeg * sizeof(uint32_t)));
 
   SeedOut so;
@@ -416,8 +452,8 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
       return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
   }
   CK(cudaEventRecord(evSeed1, ctx->st));
-  const uint32_t nPairs = h[cPairCount];
-  const uint32_t nNodes = h[cNodeCount];
+  nPairs = h[cPairCount];
+  nNodes = h[cNodeCount];
 
   // Learned filter: feature rows of every candidate pair, then their scores.
   const bool useFilter = ctx->filterOn && nPairs > 0;
@@ -438,30 +474,49 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
       CK(cudaMemsetAsync(ctx->dLogit.p, 0, (size_t)nPairs * sizeof(float), ctx->st));
     CK(cudaEventRecord(ctx->evF1, ctx->st));
   }
+  return OIC_OK;
+}
 
-  // Align every pair.
-  CK(ctx->dWork.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
-  CK(ctx->dCnt.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
-  CK(ctx->dRecPos.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
-  CK(ctx->dRec.ensure((size_t)std::max<uint32_t>(nPairs, 1) * 18 * sizeof(uint32_t)));
-  CK(ctx->dAlnOvf.ensure((size_t)std::max<uint32_t>(nPairs, 1) * sizeof(uint32_t)));
+// Per-bin figures of one align stage.
+struct AlignTimes {
+  float    msNarrow = 0, msWide = 0;
+  uint64_t pairsNarrow = 0, pairsWide = 0, cellsWide = 0;
+};
+
+// Align stage of a batch: work list by bin, the one-warp bin, the CTA bin (its own
+// pairs plus the one-warp overflow), the large-arena rerun, then the records compacted
+// into `recOut` (appended) and the counters into ctx->stats.
+int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning &tn, cudaEvent_t evAln0,
+                cudaEvent_t evAln1, std::vector<uint32_t> &recOut, AlignTimes &at) {
+  int rc = OIC_OK;
+  const bool useFilter = ctx->filterOn && nPairs > 0;
+  CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, 4 * sizeof(uint32_t), ctx->st));   // work, aln ovf, err, rec total
+  CK(cudaMemsetAsync(ctr32(ctx) + cKeep, 0, 2 * sizeof(uint32_t), ctx->st));
+  CK(cudaMemsetAsync(ctr64(ctx) + kAlignStatBase, 0, kStCount * sizeof(unsigned long long), ctx->st));
+  CK(cudaEventRecord(evAln0, ctx->st));
+  const size_t np1 = std::max<uint32_t>(nPairs, 1);
+  CK(ctx->dWork.ensure(np1 * 2 * sizeof(uint32_t)));
+  CK(ctx->dCnt.ensure(np1 * sizeof(uint32_t)));
+  CK(ctx->dRecPos.ensure(np1 * sizeof(uint32_t)));
+  CK(ctx->dRec.ensure(np1 * 18 * sizeof(uint32_t)));
+  CK(ctx->dAlnOvf.ensure(np1 * sizeof(uint32_t)));
+  uint32_t nNarrow = 0, nWide = 0;
   if (nPairs) {
-    // Pairs with the most match nodes (the most extensions) go first.
     CK(ctx->dWorkK.ensure((size_t)nPairs * 8));
     CK(ctx->dWorkK2.ensure((size_t)nPairs * 8));
     CK(ctx->dWorkV2.ensure((size_t)nPairs * 4));
     CK(ctx->dWorkScratch.ensure(radix_sort_scratch(nPairs) + 256));
     launch_work_keys(ctx->dPairs.as<PairRec>(), nPairs, useFilter ? ctx->dLogit.as<float>() : nullptr,
-                     ctx->filterLogitThr, ctr32(ctx) + cKeep, ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(),
-                     ctx->st);
+                     ctx->filterLogitThr, ctx->R.len, ctx->T.sread, tn.wideMinLen, ctr32(ctx) + cKeep,
+                     ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->st);
     CK(radix_sort_u64_u32(ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->dWorkK2.as<u64>(),
                           ctx->dWorkV2.as<uint32_t>(), nPairs, 32, ctx->dWorkScratch.p, ctx->st));
-  }
-  if (nPairs) CK(cudaMemsetAsync(ctx->dCnt.p, 0, nPairs * sizeof(uint32_t), ctx->st));
-  uint32_t nWork = nPairs;
-  if (useFilter) {   // the kept pairs lead the sorted work list
-    CK(cudaMemcpyAsync(&nWork, ctr32(ctx) + cKeep, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-    if ((rc = sync_check(ctx, "candidate filter"))) return rc;
+    CK(cudaMemsetAsync(ctx->dCnt.p, 0, nPairs * sizeof(uint32_t), ctx->st));
+    uint32_t bc[2];
+    CK(cudaMemcpyAsync(bc, ctr32(ctx) + cKeep, sizeof(bc), cudaMemcpyDeviceToHost, ctx->st));
+    if ((rc = sync_check(ctx, "work list"))) return rc;
+    nNarrow = bc[0];
+    nWide   = bc[1];
   }
   if (ctx->collect && nPairs) {
     CK(ctx->dPairCells.ensure((size_t)nPairs * sizeof(uint32_t)));
@@ -481,44 +536,77 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   const bool tier  = useFilter && ctx->filterTierThr > ctx->filterLogitThr;
   ao.tierLogit     = tier ? ctx->dLogit.as<float>() : nullptr;
   ao.tierThr       = ctx->filterTierThr;
-  AlignConfig an = align_normal(ctx);
-  WarpScratch ws;
-  if ((rc = ensure_align_scratch(ctx, an, false, ws))) return rc;
-  launch_align(an.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
-               ctx->dWork.as<uint32_t>(), nWork, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, an.caps,
-               an.warps, ao, ctx->st);
-  CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-  if ((rc = sync_check(ctx, "align kernel"))) return rc;
-  if (h[cAlnOvf] > 0) {
-    const uint32_t nOvf = h[cAlnOvf];
-    if (verbose()) fprintf(stderr, "oic: %u pairs rerun in the wide DP configuration\n", nOvf);
-    // The overflow list becomes the work list of the wide configuration.
-    CK(cudaMemcpyAsync(ctx->dWork.p, ctx->dAlnOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->st));
-    CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, sizeof(uint32_t), ctx->st));
-    CK(cudaMemsetAsync(ctr32(ctx) + cAlnOvf, 0, sizeof(uint32_t), ctx->st));
-    CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, sizeof(uint32_t), ctx->st));
-    AlignConfig aw = align_wide(ctx);
-    WarpScratch ww;
-    if ((rc = ensure_align_scratch(ctx, aw, true, ww))) return rc;
-    cudaEvent_t w0, w1;
-    cudaEventCreate(&w0);
-    cudaEventCreate(&w1);
-    cudaEventRecord(w0, ctx->st);
-    launch_align(aw.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
-                 ctx->dWork.as<uint32_t>(), nOvf, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ww, aw.caps,
-                 aw.warps, ao, ctx->st);
-    cudaEventRecord(w1, ctx->st);
+
+  cudaEvent_t ev[4];
+  for (auto &x : ev) CK(cudaEventCreate(&x));
+  struct EvGuard {
+    cudaEvent_t *e;
+    ~EvGuard() {
+      for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]);
+    }
+  } guard{ev};
+
+  // One-warp bin.
+  uint32_t h[16];
+  uint32_t nOvf = 0;
+  unsigned long long cellsAfterNarrow = 0;
+  CK(cudaEventRecord(ev[0], ctx->st));
+  if (nNarrow) {
+    AlignConfig an = align_normal(ctx);
+    an.caps.arenaCap = (int)tn.narrowArena;
+    WarpScratch ws;
+    if ((rc = ensure_align_scratch(ctx, an, false, ws))) return rc;
+    launch_align(an.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
+                 ctx->dWork.as<uint32_t>(), nNarrow, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, an.caps,
+                 an.warps, ao, ctx->st);
     CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-    if ((rc = sync_check(ctx, "align kernel (wide)"))) return rc;
-    float wms = 0;
-    cudaEventElapsedTime(&wms, w0, w1);
-    cudaEventDestroy(w0);
-    cudaEventDestroy(w1);
-    if (verbose()) fprintf(stderr, "oic: wide DP pass %.2f ms\n", wms);
-    if (h[cAlnOvf] > 0)
-      return fail(ctx, OIC_ERR_OVERFLOW, "a read pair needs a wider DP band or deeper traceback than the engine holds (err 0x%x)",
-                  h[cErr]);
+    CK(cudaMemcpyAsync(&cellsAfterNarrow, ctr64(ctx) + kAlignStatBase + kStCells, 8, cudaMemcpyDeviceToHost,
+                       ctx->st));
+    if ((rc = sync_check(ctx, "align kernel"))) return rc;
+    nOvf = h[cAlnOvf];
   }
+  CK(cudaEventRecord(ev[1], ctx->st));
+  at.pairsNarrow += nNarrow;
+
+  // CTA bin: its own pairs (after the one-warp bin in the sorted list) and the
+  // one-warp overflow appended behind them.
+  uint32_t nW = nWide + nOvf;
+  if (nW) {
+    if (nOvf) {
+      if (verbose()) fprintf(stderr, "oic: %u pairs moved from the one-warp DP to the CTA DP\n", nOvf);
+      CK(cudaMemcpyAsync(ctx->dWork.as<uint32_t>() + nNarrow + nWide, ctx->dAlnOvf.p, nOvf * sizeof(uint32_t),
+                         cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    for (int level = 0; level < 2 && nW; level++) {
+      const bool huge = level == 1;
+      CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, sizeof(uint32_t), ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cAlnOvf, 0, sizeof(uint32_t), ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, sizeof(uint32_t), ctx->st));
+      uint32_t    ctas = 0;
+      AlignCaps   caps;
+      WarpScratch ws;
+      if ((rc = ensure_group_scratch(ctx, tn, huge, ctas, caps, ws))) return rc;
+      const int threads = huge ? (int)std::max<uint32_t>(tn.wideThreads, 512) : (int)tn.wideThreads;
+      launch_align_group(threads, (int)tn.wideTile, caps.bandW, (int)std::min<uint32_t>(ctas, nW), ctx->R, ctx->T,
+                         ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
+                         ctx->dWork.as<uint32_t>() + nNarrow, nW, ctr32(ctx) + cWorkCounter,
+                         ctx->dNodes.as<int4>(), ws, caps, ao, ctx->st);
+      CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+      if ((rc = sync_check(ctx, huge ? "align kernel (large arena)" : "align kernel (CTA bin)"))) return rc;
+      at.pairsWide += nW;
+      const uint32_t o = h[cAlnOvf];
+      if (o && huge)
+        return fail(ctx, OIC_ERR_OVERFLOW,
+                    "a read pair needs a wider DP band or deeper traceback than the engine holds (err 0x%x)", h[cErr]);
+      if (o) {
+        if (verbose()) fprintf(stderr, "oic: %u pairs rerun with the large DP arena\n", o);
+        CK(cudaMemcpyAsync(ctx->dWork.as<uint32_t>() + nNarrow, ctx->dAlnOvf.p, o * sizeof(uint32_t),
+                           cudaMemcpyDeviceToDevice, ctx->st));
+      }
+      nW = o;
+    }
+  }
+  CK(cudaEventRecord(ev[2], ctx->st));
   CK(cudaEventRecord(evAln1, ctx->st));
 
   // Compact the records and bring them home.
@@ -532,9 +620,9 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
     CK(ctx->dRecOut.ensure((size_t)nRec * 6 * sizeof(uint32_t)));
     launch_compact_records(ctx->dRec.as<uint32_t>(), ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), nPairs,
                            ctx->dRecOut.as<uint32_t>(), ctx->st);
-    size_t old = ctx->out.size();
-    ctx->out.resize(old + (size_t)nRec * 6);
-    CK(cudaMemcpyAsync(ctx->out.data() + old, ctx->dRecOut.p, (size_t)nRec * 6 * sizeof(uint32_t),
+    size_t old = recOut.size();
+    recOut.resize(old + (size_t)nRec * 6);
+    CK(cudaMemcpyAsync(recOut.data() + old, ctx->dRecOut.p, (size_t)nRec * 6 * sizeof(uint32_t),
                        cudaMemcpyDeviceToHost, ctx->st));
   }
   unsigned long long st64[2 + kStCount];
@@ -542,18 +630,12 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   CK(cudaMemcpyAsync(st64 + 2, ctr64(ctx) + kAlignStatBase, kStCount * sizeof(unsigned long long),
                      cudaMemcpyDeviceToHost, ctx->st));
   if ((rc = sync_check(ctx, "record compaction"))) return rc;
-
-  float a = 0, b = 0;
-  cudaEventElapsedTime(&a, evSeed0, evSeed1);
-  cudaEventElapsedTime(&b, evSeed1, evAln1);
-  msSeed += a;
-  msAlign += b;
-  if ((useFilter || ctx->collect) && nPairs) {
-    float f = 0;
-    cudaEventElapsedTime(&f, ctx->evF0, ctx->evF1);
-    ctx->stats.msFilter += f;
-  }
-  if (ctx->collect && nPairs && (rc = collect_batch(ctx, nPairs, nNodes, useFilter))) return rc;
+  float a0 = 0, a1 = 0;
+  cudaEventElapsedTime(&a0, ev[0], ev[1]);
+  cudaEventElapsedTime(&a1, ev[1], ev[2]);
+  at.msNarrow += a0;
+  at.msWide += a1;
+  at.cellsWide += st64[2 + kStCells] - cellsAfterNarrow;
 
   oic_stats &S = ctx->stats;
   S.seeds += st64[0];
@@ -571,8 +653,79 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   S.extensions += st64[2 + kStExtensions];
   S.dpRows += st64[2 + kStRows];
   S.dpCellsNoOverlap += st64[2 + kStCellsNoOlap];
-  if (useFilter) S.filteredPairs += nPairs - nWork;
+  if (useFilter) S.filteredPairs += nPairs - nNarrow - nWide;
   return OIC_OK;
+}
+
+// Process one batch of eligible ref reads against the loaded block.  Returns OIC_OK,
+// or kRetrySmaller when the batch's output did not fit (caller splits the batch).
+int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
+              cudaEvent_t evAln1, float &msSeed, float &msAlign) {
+  uint32_t nPairs = 0, nNodes = 0;
+  int rc = seed_stage(ctx, refs, nRefs, evSeed0, evSeed1, nPairs, nNodes);
+  if (rc) return rc;
+  const bool useFilter = ctx->filterOn && nPairs > 0;
+  const oic_tuning tn = resolved_tuning(ctx);
+  AlignTimes at;
+  if ((rc = align_stage(ctx, nPairs, nNodes, tn, evSeed1, evAln1, ctx->out, at))) return rc;
+  float a = 0, b = 0;
+  cudaEventElapsedTime(&a, evSeed0, evSeed1);
+  cudaEventElapsedTime(&b, evSeed1, evAln1);
+  msSeed += a;
+  msAlign += b;
+  oic_stats &S = ctx->stats;
+  S.msNarrow += at.msNarrow;
+  S.msWide += at.msWide;
+  S.pairsNarrow += at.pairsNarrow;
+  S.pairsWide += at.pairsWide;
+  S.cellsWide += at.cellsWide;
+  if ((useFilter || ctx->collect) && nPairs) {
+    float f = 0;
+    cudaEventElapsedTime(&f, ctx->evF0, ctx->evF1);
+    S.msFilter += f;
+  }
+  if (ctx->collect && nPairs && (rc = collect_batch(ctx, nPairs, nNodes, useFilter))) return rc;
+  return OIC_OK;
+}
+
+// 0-based indices of the ref reads of [bgnRefID, endRefID] that Process_Overlaps
+// scans (Process_Overlaps.C:50-55: library range and minimum overlap length).
+int eligible_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, std::vector<uint32_t> &refs) {
+  const oic_params &P = ctx->P;
+  if (bgnRefID < 1) bgnRefID = 1;
+  if (endRefID > ctx->nReads) endRefID = ctx->nReads;
+  for (uint64_t id = bgnRefID; id <= endRefID; id++) {
+    const uint32_t r = (uint32_t)id - 1;
+    if (ctx->lib[r] < P.minLibToRef || ctx->lib[r] > P.maxLibToRef) continue;
+    if ((int64_t)ctx->len[r] < (int64_t)P.minOlapLen) continue;
+    if (ctx->len[r] < P.kmerLen) return fail(ctx, OIC_ERR_INPUT, "read %u is shorter than the k-mer size", (uint32_t)id);
+    refs.push_back(r);
+  }
+  return OIC_OK;
+}
+
+// Output capacities of a batch, sized once from the free memory.
+int ensure_pair_caps(oic_ctx *ctx) {
+  if (ctx->pairCap) return OIC_OK;
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  // Per pair: the record (32 B), three output slots (72 B) and the work-list, count and
+  // position words; per node 16 B.  Take about a fifth of the free memory.
+  const size_t budget = freeB / 5;
+  size_t pc = std::min<size_t>(32u << 20, budget / 3 / 160), nc = std::min<size_t>(1u << 29, budget * 2 / 3 / 16);
+  ctx->pairCap = (uint32_t)std::max<size_t>(pc, 1u << 16);
+  ctx->nodeCap = (uint32_t)std::max<size_t>(nc, 1u << 20);
+  CK(ctx->dPairs.ensure((size_t)ctx->pairCap * sizeof(PairRec)));
+  CK(ctx->dNodes.ensure((size_t)ctx->nodeCap * sizeof(int4)));
+  return OIC_OK;
+}
+
+// CTAs of the CTA bin: as many per SM (at most 2) as the row buffers leave room for
+// in the SM's 227 KB of shared memory.
+uint32_t resolved_tuning_ctas(const oic_ctx *c, const oic_tuning &t) {
+  const size_t per = (size_t)2 * t.wideBandW * sizeof(int) + 4096;
+  const int    k   = (int)std::max<size_t>(1, std::min<size_t>(2, (227u << 10) / per));
+  return (uint32_t)(k * c->nSM);
 }
 
 }  // namespace
@@ -980,32 +1133,11 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
   if (!ctx) return OIC_ERR_ARG;
   if (!ctx->haveBlock) return fail(ctx, OIC_ERR_STATE, "no hash block loaded");
   cudaSetDevice(ctx->device);
-  const oic_params &P = ctx->P;
-  if (bgnRefID < 1) bgnRefID = 1;
-  if (endRefID > ctx->nReads) endRefID = ctx->nReads;
   std::vector<uint32_t> refs;
-  for (uint64_t id = bgnRefID; id <= endRefID; id++) {
-    const uint32_t r = (uint32_t)id - 1;
-    if (ctx->lib[r] < P.minLibToRef || ctx->lib[r] > P.maxLibToRef) continue;     // Process_Overlaps.C:50-55
-    if ((int64_t)ctx->len[r] < (int64_t)P.minOlapLen) continue;
-    if (ctx->len[r] < P.kmerLen) return fail(ctx, OIC_ERR_INPUT, "read %u is shorter than the k-mer size", (uint32_t)id);
-    refs.push_back(r);
-  }
+  int erc = eligible_refs(ctx, bgnRefID, endRefID, refs);
+  if (erc) return erc;
   if (refs.empty()) return OIC_OK;
-
-  // Output capacities for a batch.
-  size_t freeB = 0, totalB = 0;
-  cudaMemGetInfo(&freeB, &totalB);
-  if (ctx->pairCap == 0) {
-    // Per pair: the record (32 B), three output slots (72 B) and the work-list,
-    // count and position words; per node 16 B.  Take about a fifth of the free memory.
-    const size_t budget = freeB / 5;
-    size_t pc = std::min<size_t>(32u << 20, budget / 3 / 160), nc = std::min<size_t>(1u << 29, budget * 2 / 3 / 16);
-    ctx->pairCap = (uint32_t)std::max<size_t>(pc, 1u << 16);
-    ctx->nodeCap = (uint32_t)std::max<size_t>(nc, 1u << 20);
-    CK(ctx->dPairs.ensure((size_t)ctx->pairCap * sizeof(PairRec)));
-    CK(ctx->dNodes.ensure((size_t)ctx->nodeCap * sizeof(int4)));
-  }
+  if ((erc = ensure_pair_caps(ctx))) return erc;
 
   cudaEvent_t e0, e1, e2;
   cudaEventCreate(&e0);
@@ -1206,36 +1338,240 @@ int oic_extend_batch(oic_ctx *ctx, uint32_t nAlign, const uint32_t *sRead, const
   CK(cudaMemsetAsync(ctr64(ctx) + kExtStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
   std::vector<uint32_t> status(nAlign);
   int rc = OIC_OK;
-  for (int pass = 0; pass < 2 && rc == OIC_OK; pass++) {
+  const oic_tuning tn = resolved_tuning(ctx);
+  // Pass 0: one warp per problem; pass 1: one CTA per problem (every problem when the
+  // tuning forces the CTA bin, else those that overflowed); pass 2: the large arena.
+  DevBuf dSub;
+  std::vector<uint32_t> idx;
+  for (int pass = tn.forceWide ? 1 : 0; pass < 3 && rc == OIC_OK; pass++) {
     CK(cudaMemsetAsync(ctr64(ctx) + kExtStatBase, 0, 2 * sizeof(unsigned long long), ctx->st));
-    AlignConfig ac = pass == 0 ? align_normal(ctx) : align_wide(ctx);
-    WarpScratch ws;
-    if ((rc = ensure_align_scratch(ctx, ac, pass == 1, ws))) break;
-    launch_extend_batch(ac.bandW, ctx->R, ctx->dp, ctx->dEml.as<int>(), dP.as<ExtendProblem>(), nAlign, ws, ac.caps,
-                        ac.warps, dOut.as<int>(), dKind.as<int>(), dDl.as<int>(), dStatus.as<uint32_t>(),
-                        ctr64(ctx) + kExtStatBase, ctx->st);
+    if (pass == 0) {
+      AlignConfig ac = align_normal(ctx);
+      ac.caps.arenaCap = (int)tn.narrowArena;
+      WarpScratch ws;
+      if ((rc = ensure_align_scratch(ctx, ac, false, ws))) break;
+      launch_extend_batch(ac.bandW, ctx->R, ctx->dp, ctx->dEml.as<int>(), dP.as<ExtendProblem>(), nAlign, ws,
+                          ac.caps, ac.warps, dOut.as<int>(), dKind.as<int>(), dDl.as<int>(), dStatus.as<uint32_t>(),
+                          ctr64(ctx) + kExtStatBase, ctx->st);
+    } else {
+      // The problems still open run in a compact sub-batch; results are scattered back.
+      std::vector<ExtendProblem> sub;
+      idx.clear();
+      for (uint32_t i = 0; i < nAlign; i++)
+        if (pass == 1 ? (tn.forceWide || status[i] != 0) : status[i] != 0) {
+          idx.push_back(i);
+          sub.push_back(pb[i]);
+        }
+      const uint32_t ns = (uint32_t)sub.size();
+      CK(dSub.ensure((size_t)ns * (sizeof(ExtendProblem) + 8 * 4)));
+      ExtendProblem *sp = dSub.as<ExtendProblem>();
+      int *so = (int *)(sp + ns), *sk = so + 5 * (size_t)ns, *sd = sk + ns;
+      uint32_t *ss = (uint32_t *)(sd + ns);
+      CK(cudaMemcpyAsync(sp, sub.data(), ns * sizeof(ExtendProblem), cudaMemcpyHostToDevice, ctx->st));
+      uint32_t    ctas = 0;
+      AlignCaps   caps;
+      WarpScratch ws;
+      if ((rc = ensure_group_scratch(ctx, tn, pass == 2, ctas, caps, ws))) break;
+      const int threads = pass == 2 ? (int)std::max<uint32_t>(tn.wideThreads, 512) : (int)tn.wideThreads;
+      launch_extend_group(threads, (int)tn.wideTile, caps.bandW, (int)std::min<uint32_t>(ctas, ns), ctx->R, ctx->dp,
+                          ctx->dEml.as<int>(), sp, ns, ws, caps, so, sk, sd, ss, ctr64(ctx) + kExtStatBase, ctx->st);
+      std::vector<int32_t> o5((size_t)ns * 5), ok(ns), od(ns);
+      std::vector<uint32_t> os(ns);
+      CK(cudaMemcpyAsync(o5.data(), so, (size_t)ns * 20, cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(ok.data(), sk, (size_t)ns * 4, cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(od.data(), sd, (size_t)ns * 4, cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(os.data(), ss, (size_t)ns * 4, cudaMemcpyDeviceToHost, ctx->st));
+      if ((rc = sync_check(ctx, "extend batch (CTA bin)"))) break;
+      // Scatter into the full-size device outputs.
+      std::vector<int32_t> f5((size_t)nAlign * 5), fk(nAlign), fd(nAlign);
+      CK(cudaMemcpy(f5.data(), dOut.p, (size_t)nAlign * 20, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(fk.data(), dKind.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(fd.data(), dDl.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
+      for (uint32_t q = 0; q < ns; q++) {
+        const uint32_t i = idx[q];
+        for (int k = 0; k < 5; k++) f5[(size_t)i * 5 + k] = o5[(size_t)q * 5 + k];
+        fk[i]     = ok[q];
+        fd[i]     = od[q];
+        status[i] = os[q];
+      }
+      CK(cudaMemcpy(dOut.p, f5.data(), (size_t)nAlign * 20, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dKind.p, fk.data(), (size_t)nAlign * 4, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(dDl.p, fd.data(), (size_t)nAlign * 4, cudaMemcpyHostToDevice));
+      unsigned long long s2[2];
+      CK(cudaMemcpy(s2, ctr64(ctx) + kExtStatBase, sizeof(s2), cudaMemcpyDeviceToHost));
+      ctx->stats.dpCells += s2[0];
+      ctx->stats.slideBases += s2[1];
+      bool any = false;
+      for (uint32_t q = 0; q < ns; q++) any |= os[q] != 0;
+      if (!any) break;
+      if (pass == 2) rc = fail(ctx, OIC_ERR_OVERFLOW, "an alignment exceeds the engine's DP capacity");
+      continue;
+    }
     CK(cudaMemcpyAsync(status.data(), dStatus.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost, ctx->st));
     if ((rc = sync_check(ctx, "extend batch"))) break;
+    unsigned long long s2[2];
+    CK(cudaMemcpy(s2, ctr64(ctx) + kExtStatBase, sizeof(s2), cudaMemcpyDeviceToHost));
+    ctx->stats.dpCells += s2[0];
+    ctx->stats.slideBases += s2[1];
     bool any = false;
     for (uint32_t i = 0; i < nAlign; i++) any |= status[i] != 0;
     if (!any) break;
-    if (pass == 1) rc = fail(ctx, OIC_ERR_OVERFLOW, "an alignment exceeds the engine's DP capacity");
   }
   if (rc == OIC_OK) {
     CK(cudaMemcpy(out, dOut.p, (size_t)nAlign * 5 * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(kind, dKind.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(deltaLen, dDl.p, (size_t)nAlign * 4, cudaMemcpyDeviceToHost));
-    unsigned long long s2[2];
-    CK(cudaMemcpy(s2, ctr64(ctx) + kExtStatBase, sizeof(s2), cudaMemcpyDeviceToHost));
-    ctx->stats.dpCells += s2[0];
-    ctx->stats.slideBases += s2[1];
   }
   dP.release();
+  dSub.release();
   dOut.release();
   dKind.release();
   dDl.release();
   dStatus.release();
   return rc;
+}
+
+int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (!t) {
+    ctx->tune = oic_tuning{};
+    return OIC_OK;
+  }
+  if (t->wideThreads && (t->wideThreads < 64 || t->wideThreads > 512 || t->wideThreads % 32))
+    return fail(ctx, OIC_ERR_ARG, "wideThreads must be a multiple of 32 in [64, 512]");
+  if (t->wideTile && t->wideTile != 1 && t->wideTile != 2 && t->wideTile != 4)
+    return fail(ctx, OIC_ERR_ARG, "wideTile must be 1, 2 or 4");
+  if (t->wideBandW && (t->wideBandW < 512 || (size_t)t->wideBandW * 8 > (200u << 10)))
+    return fail(ctx, OIC_ERR_ARG, "wideBandW must be in [512, 25600]");
+  if (t->narrowArena && t->narrowArena < (1u << 16))
+    return fail(ctx, OIC_ERR_ARG, "narrowArena must be at least 65536 cells");
+  if (t->wideArena && (t->wideArena < (1u << 20) || t->wideArena > 0x7fff0000ull))
+    return fail(ctx, OIC_ERR_ARG, "wideArena must be in [2^20, 2^31) cells");
+  ctx->tune = *t;
+  return OIC_OK;
+}
+
+int oic_get_tuning(oic_ctx *ctx, oic_tuning *t) {
+  if (!ctx || !t) return OIC_ERR_ARG;
+  *t = resolved_tuning(ctx);
+  return OIC_OK;
+}
+
+int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *report, uint32_t maxReport,
+                 uint32_t *nReport) {
+  if (!ctx) return OIC_ERR_ARG;
+  if (!ctx->haveBlock) return fail(ctx, OIC_ERR_STATE, "no hash block loaded");
+  cudaSetDevice(ctx->device);
+  std::vector<uint32_t> refs;
+  int rc = eligible_refs(ctx, bgnRefID, endRefID, refs);
+  if (rc) return rc;
+  if (refs.empty()) return fail(ctx, OIC_ERR_ARG, "no eligible ref reads in %u-%u", bgnRefID, endRefID);
+  if ((rc = ensure_pair_caps(ctx))) return rc;
+  const oic_stats saved   = ctx->stats;
+  const size_t    outMark = ctx->out.size();
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  uint32_t nPairs = 0, nNodes = 0;
+  rc = seed_stage(ctx, refs.data(), (uint32_t)refs.size(), e0, e1, nPairs, nNodes);
+  if (rc == kRetrySmaller) rc = fail(ctx, OIC_ERR_OVERFLOW, "the autotune sample's candidate pairs do not fit");
+
+  // Length-bin boundaries to try: quantiles of the pairs' shorter read.
+  std::vector<uint32_t> minLen;
+  if (!rc && nPairs) {
+    std::vector<PairRec> pr(nPairs);
+    CK(cudaMemcpy(pr.data(), ctx->dPairs.p, (size_t)nPairs * sizeof(PairRec), cudaMemcpyDeviceToHost));
+    minLen.resize(nPairs);
+    for (uint32_t i = 0; i < nPairs; i++)
+      minLen[i] = std::min(ctx->len[pr[i].sRead], ctx->len[ctx->blkFirst - 1 + pr[i].tStr]);
+    std::sort(minLen.begin(), minLen.end());
+  }
+
+  struct Line {
+    oic_tuning t;
+    AlignTimes at;
+  };
+  std::vector<Line>     lines;
+  std::vector<uint32_t> ref0;
+  bool                  haveRef = false;
+  oic_tuning base       = resolved_tuning(ctx);
+  base.forceWide        = 0;
+  auto measure = [&](oic_tuning t) -> int {
+    std::vector<uint32_t> recs;
+    AlignTimes at;
+    int r = align_stage(ctx, nPairs, nNodes, t, e1, e2, recs, at);
+    if (r) return r;
+    if (!haveRef) {
+      ref0    = recs;
+      haveRef = true;
+    } else if (recs != ref0) {
+      return fail(ctx, OIC_ERR_DEVICE, "DP configurations disagree on the records (threads %u, tile %u)",
+                  t.wideThreads, t.wideTile);
+    }
+    lines.push_back(Line{t, at});
+    return OIC_OK;
+  };
+  auto total = [](const Line &l) { return (double)l.at.msNarrow + l.at.msWide; };
+  if (!rc && nPairs) {
+    // Stage 1: warps per pair x tile width of the CTA bin, no length bin.
+    const uint32_t threadsGrid[] = {64, 128, 256, 512};
+    const uint32_t tileGrid[]    = {1, 2, 4};
+    for (uint32_t th : threadsGrid)
+      for (uint32_t tl : tileGrid) {
+        oic_tuning t  = base;
+        t.wideThreads = th;
+        t.wideTile    = tl;
+        t.wideMinLen  = 0xffffffffu;
+        t.wideCtas    = 0;
+        t.wideCtas    = resolved_tuning_ctas(ctx, t);
+        if ((rc = measure(t))) break;
+      }
+    // Stage 2: the length-bin boundary with the best CTA configuration.
+    if (!rc) {
+      size_t best = 0;
+      for (size_t i = 1; i < lines.size(); i++)
+        if (total(lines[i]) < total(lines[best])) best = i;
+      const double qs[] = {0.5, 0.9, 0.99, 0.999};
+      for (double q : qs) {
+        oic_tuning t = lines[best].t;
+        t.wideMinLen = std::max<uint32_t>(1, minLen[(size_t)(q * (minLen.size() - 1))]);
+        if ((rc = measure(t))) break;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  ctx->stats = saved;
+  ctx->out.resize(outMark);
+  if (rc) return rc;
+  if (!lines.empty()) {
+    size_t best = 0;
+    for (size_t i = 1; i < lines.size(); i++)
+      if (total(lines[i]) < total(lines[best])) best = i;
+    ctx->tune = lines[best].t;
+    if (verbose())
+      fprintf(stderr, "oic: autotune: %zu configurations on %u pairs; best: %u threads, tile %u, length bin %u (%.1f ms)\n",
+              lines.size(), nPairs, ctx->tune.wideThreads, ctx->tune.wideTile, ctx->tune.wideMinLen,
+              total(lines[best]));
+  }
+  uint32_t k = 0;
+  for (const Line &l : lines) {
+    if (!report || k >= maxReport) break;
+    double *r = report + (size_t)k * 8;
+    r[0] = l.t.wideTile;
+    r[1] = l.t.wideThreads;
+    r[2] = l.t.wideMinLen == 0xffffffffu ? -1.0 : (double)l.t.wideMinLen;
+    r[3] = l.at.msNarrow;
+    r[4] = l.at.msWide;
+    r[5] = total(l);
+    r[6] = (double)(l.at.pairsNarrow);
+    r[7] = (double)l.at.cellsWide;
+    k++;
+  }
+  if (nReport) *nReport = report ? k : (uint32_t)lines.size();
+  return OIC_OK;
 }
 
 }  // extern "C"

@@ -101,10 +101,22 @@ enum StatIdx {
   kStCells, kStSlides, kStExtensions, kStRows, kStCellsNoOlap, kStCount
 };
 
-// bandW selects the shared-memory configuration (compiled instances: 512, 8192).
+// One pair per warp, 8 warps per CTA, 512-int shared-memory rows (bandW is ignored).
 void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs,
                   const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap,
                   int nWarps, AlignOut out, cudaStream_t st);
+
+// One pair per CTA of `threads` threads (a multiple of 32, at most 512): warp 0 runs
+// the pair logic and the whole CTA runs each error-row loop, U (1, 2, 4) diagonals per
+// thread per pass; row buffers of bandW ints in shared memory; scratch per CTA.
+void launch_align_group(int threads, int U, int bandW, int ctas, ReadsDev R, TableDev T, DevParams P, const int *eml,
+                        const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes,
+                        WarpScratch sc, AlignCaps cap, AlignOut out, cudaStream_t st);
+
+struct ExtendProblem;
+void launch_extend_group(int threads, int U, int bandW, int ctas, ReadsDev R, DevParams P, const int *eml,
+                         const ExtendProblem *probs, u32 n, WarpScratch sc, AlignCaps cap, int *out, int *kind,
+                         int *deltaLen, u32 *status, unsigned long long *stats, cudaStream_t st);
 
 struct ExtendProblem {
   u32 sRead, sRev, tRead;
@@ -114,11 +126,13 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
                          WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
                          unsigned long long *stats, cudaStream_t st);
 
-// Sort keys that put the pairs with the most match nodes first.  With a filter score
-// (logit non-null) a pair whose score is below logitThr gets the largest key, so the
-// kept pairs come first; keepCount (zeroed by the caller) gets their number.
-void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
-                      unsigned long long *keys, u32 *vals, cudaStream_t st);
+// Sort keys (32 bits) of the work list: by bin -- 0 one-warp DP, 1 CTA DP (shorter read
+// >= wideMinLen bases), 2 dropped by the filter (logit non-null, below logitThr) -- and
+// inside a bin the pairs with the most match nodes first.  binCount[0..1] (zeroed by
+// the caller) get the sizes of bins 0 and 1.
+void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
+                      const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys, u32 *vals,
+                      cudaStream_t st);
 
 // ---------------- learned candidate filter (oic_filter.cu) ----------------
 // feat: n x 80 FP16 rows (67 features, 13 zeros) of the candidate pairs.

@@ -22,7 +22,6 @@ namespace oic {
 namespace {
 
 constexpr int kAlignWarpsSmall = 8;   // bandW 512
-constexpr int kAlignWarpsLarge = 1;   // bandW 8192
 
 struct Olap {
   int    s_lo, s_hi, t_lo, t_hi;
@@ -246,6 +245,7 @@ __device__ void output_partial(u32 *dst, u32 sID, u32 tID, int rev, const Olap &
 
 // Process_Matches for one pair.  Counts go to ps.pc, records (lane 0) to recOut.
 // Returns false on a capacity overflow: the caller then discards ps.pc and the records.
+template <bool GROUP>
 __device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const TableDev &Tb, const PairRec &pr,
                              const int4 *nodesAll, u32 *recOut, u32 &nRec, int extLimit) {
   const int lane = threadIdx.x & 31;
@@ -345,7 +345,7 @@ __device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const T
     const int4 lm = nodes[li];
 
     int sLo = 0, sHi = 0, tLo = 0, tHi = 0, errors = 0;
-    const int kind = warp_extend(w, S, sLen, T, tLen, lm.z, lm.x, lm.y, sLo, sHi, tLo, tHi, errors);
+    const int kind = warp_extend<GROUP>(w, S, sLen, T, tLen, lm.z, lm.x, lm.y, sLo, sHi, tLo, tHi, errors);
     if (w.err) {
       w.cells  = cells0;
       w.slides = slides0;
@@ -419,29 +419,12 @@ __device__ bool process_pair(WarpDP &w, PairSmem &ps, const ReadsDev &R, const T
   return true;
 }
 
-template <int BANDW, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
-                                                           const PairRec *pairs, const u32 *work, u32 nWork,
-                                                           u32 *workCounter, const int4 *nodes, WarpScratch scBase,
-                                                           AlignCaps cap, AlignOut out) {
-  extern __shared__ int smemRows[];
-  __shared__ PairSmem pairSmem[WARPS];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const u64 gw   = (u64)blockIdx.x * WARPS + wib;
-  PairSmem &ps   = pairSmem[wib];
-
-  WarpDP w;
-  w.sc     = warp_scratch(scBase, cap, gw);
-  w.cap    = cap;
-  w.smA    = smemRows + (size_t)wib * 2 * BANDW;
-  w.smB    = w.smA + BANDW;
-  w.eml    = eml;
-  w.P      = P;
-  w.cells  = 0;
-  w.slides = 0;
-  w.rows   = 0;
-  w.err    = 0;
-  w.leftLen = w.rightLen = 0;
+// The work loop of one warp: pairs from the shared work list until it is empty.
+template <bool GROUP>
+static __device__ __forceinline__ void align_loop(WarpDP &w, PairSmem &ps, const ReadsDev &R, const TableDev &Tb,
+                                                  const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter,
+                                                  const int4 *nodes, const AlignOut &out) {
+  const int lane = threadIdx.x & 31;
   if (lane == 0)
     for (int i = 0; i < kStCount; i++) ps.acc.v[i] = 0;
   __syncwarp();
@@ -458,7 +441,7 @@ __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(
     const unsigned long long cellsBefore = w.cells;
     int extLimit = 0;   // 0: every match node may be extended (the reference's rule)
     if (out.tierLogit && out.tierLogit[pi] < out.tierThr) extLimit = 1;
-    const bool ok = process_pair(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, extLimit);
+    const bool ok = process_pair<GROUP>(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, extLimit);
     if (lane == 0) {
       if (ok) {
         if (nRec == 0) ps.pc.v[kStCellsNoOlap] += w.cells - cellsBefore;
@@ -490,22 +473,81 @@ __global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(
   }
 }
 
-// Longest work first: key = ~(match nodes of the pair), value = pair index.  Pairs
-// the filter drops get key 0xffffffff (every kept pair has at least one node).
-__global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
-                                 unsigned long long *keys, u32 *vals) {
+// One pair per warp, WARPS warps per CTA.
+template <int BANDW, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
+                                                           const PairRec *pairs, const u32 *work, u32 nWork,
+                                                           u32 *workCounter, const int4 *nodes, WarpScratch scBase,
+                                                           AlignCaps cap, AlignOut out) {
+  extern __shared__ int smemRows[];
+  __shared__ PairSmem pairSmem[WARPS];
+  const int wib = threadIdx.x >> 5;
+  const u64 gw  = (u64)blockIdx.x * WARPS + wib;
+  WarpDP w;
+  int *smA = smemRows + (size_t)wib * 2 * BANDW;
+  warp_dp_init(w, warp_scratch(scBase, cap, gw), cap, smA, smA + BANDW, eml, P);
+  align_loop<false>(w, pairSmem[wib], R, Tb, pairs, work, nWork, workCounter, nodes, out);
+}
+
+// One pair per CTA (the wide bins): warp 0 runs the pair logic, and every error-row
+// loop runs on all blockDim.x threads (group_rows, U diagonals per thread per pass);
+// the other warps wait for row loops in group_worker.  The row buffers are
+// cap.bandW ints each in dynamic shared memory.  Scratch is per CTA.
+__global__ void __launch_bounds__(512, 1) align_group_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
+                                                              const PairRec *pairs, const u32 *work, u32 nWork,
+                                                              u32 *workCounter, const int4 *nodes, WarpScratch scBase,
+                                                              AlignCaps cap, AlignOut out, int U) {
+  extern __shared__ int smemRows[];
+  __shared__ PairSmem    pairSmem;
+  __shared__ GroupShared gs;
+  const WarpScratch sc = warp_scratch(scBase, cap, blockIdx.x);
+  if (threadIdx.x >= 32) {
+    unsigned long long slides = 0;
+    group_worker(gs, sc, cap, eml, slides);
+    slides = warp_sum64(slides);
+    if ((threadIdx.x & 31) == 0 && slides) atomicAdd(&out.stats[kStSlides], slides);
+    return;
+  }
+  WarpDP w;
+  warp_dp_init(w, sc, cap, smemRows, smemRows + cap.bandW, eml, P);
+  w.gs       = &gs;
+  w.gThreads = blockDim.x;
+  w.gU       = U;
+  align_loop<true>(w, pairSmem, R, Tb, pairs, work, nWork, workCounter, nodes, out);
+  if (threadIdx.x == 0) gs.cmd = kGroupExit;
+  __syncwarp();
+  group_bar(1, blockDim.x);
+}
+
+// Work list order: key = bin << 30 | (2^30 - 1 - match nodes), value = pair index, so
+// the pairs sort by bin and, inside a bin, the pairs with the most match nodes (the most
+// extensions) come first.  Bin 0: the one-warp DP; bin 1: the CTA DP, for pairs whose
+// shorter read has at least wideMinLen bases; bin 2: dropped by the filter (logit
+// non-null and below logitThr).  binCount[0..1] (zeroed by the caller) get the sizes
+// of bins 0 and 1.
+__global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
+                                 const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys,
+                                 u32 *vals) {
   const u32 stride = gridDim.x * blockDim.x;
+  const int lane   = threadIdx.x & 31;
   for (u32 i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-    const u32 i    = i0 + threadIdx.x;
-    bool      keep = false;
+    const u32 i   = i0 + threadIdx.x;
+    u32       bin = 3;
     if (i < n) {
-      keep    = !logit || !(logit[i] < logitThr);
-      keys[i] = keep ? 0xffffffffull - (unsigned long long)pairs[i].nodeCnt : 0xffffffffull;
-      vals[i] = i;
+      const PairRec pr = pairs[i];
+      if (logit && logit[i] < logitThr) bin = 2;
+      else {
+        const u32 ls = readLen[pr.sRead], lt = readLen[strRead[pr.tStr]];
+        bin          = (ls < lt ? ls : lt) >= wideMinLen ? 1 : 0;
+      }
+      const u32 nc = pr.nodeCnt < 0x3fffffffu ? pr.nodeCnt : 0x3fffffffu;
+      keys[i]      = ((unsigned long long)bin << 30) | (0x3fffffffu - nc);
+      vals[i]      = i;
     }
-    if (logit) {
-      const unsigned b = __ballot_sync(0xffffffffu, keep);
-      if ((threadIdx.x & 31) == 0 && b) atomicAdd(keepCount, (u32)__popc(b));
+    const unsigned b0 = __ballot_sync(0xffffffffu, bin == 0), b1 = __ballot_sync(0xffffffffu, bin == 1);
+    if (lane == 0) {
+      if (b0) atomicAdd(&binCount[0], (u32)__popc(b0));
+      if (b1) atomicAdd(&binCount[1], (u32)__popc(b1));
     }
   }
 }
@@ -519,61 +561,67 @@ __global__ void compact_records_kernel(const u32 *rec, const u32 *cnt, const u32
 
 }  // namespace
 
-int align_warps_per_block(int bandW) { return bandW <= 512 ? kAlignWarpsSmall : kAlignWarpsLarge; }
+int align_warps_per_block(int) { return kAlignWarpsSmall; }
 
-size_t align_smem_bytes(int bandW) {
-  const int b = bandW <= 512 ? 512 : 8192;
-  return (size_t)align_warps_per_block(bandW) * 2 * b * sizeof(int);
-}
+size_t align_smem_bytes(int) { return (size_t)kAlignWarpsSmall * 2 * 512 * sizeof(int); }
 
-void launch_align(int bandW, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs, const u32 *work,
+void launch_align(int, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs, const u32 *work,
                   u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap, int nWarps,
                   AlignOut out, cudaStream_t st) {
   if (nWork == 0) return;
-  const int wpb = align_warps_per_block(bandW);
-  const int blocks = (nWarps + wpb - 1) / wpb;
-  const size_t smem = align_smem_bytes(bandW);
-  cap.bandW = bandW <= 512 ? 512 : 8192;
-  if (bandW <= 512) {
-    auto k = align_kernel<512, kAlignWarpsSmall>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
+  const int    blocks = (nWarps + kAlignWarpsSmall - 1) / kAlignWarpsSmall;
+  const size_t smem   = align_smem_bytes(512);
+  cap.bandW           = 512;
+  auto k = align_kernel<512, kAlignWarpsSmall>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<blocks, kAlignWarpsSmall * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
   g_launches++;
-  } else {
-    auto k = align_kernel<8192, kAlignWarpsLarge>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<blocks, wpb * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
-  g_launches++;
-  }
 }
 
-void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
+void launch_align_group(int threads, int U, int bandW, int ctas, ReadsDev R, TableDev T, DevParams P, const int *eml,
+                        const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes,
+                        WarpScratch sc, AlignCaps cap, AlignOut out, cudaStream_t st) {
+  if (nWork == 0) return;
+  cap.bandW         = bandW;
+  const size_t smem = (size_t)2 * bandW * sizeof(int);
+  cudaFuncSetAttribute(align_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  align_group_kernel<<<ctas, threads, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out,
+                                                  U);
+  g_launches++;
+}
+
+void launch_extend_batch(int, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
                          WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,
                          unsigned long long *stats, cudaStream_t st) {
   if (n == 0) return;
-  const int wpb = align_warps_per_block(bandW);
-  const int blocks = (nWarps + wpb - 1) / wpb;
-  const size_t smem = align_smem_bytes(bandW);
-  cap.bandW = bandW <= 512 ? 512 : 8192;
-  if (bandW <= 512) {
-    auto k = extend_batch_kernel<512, kAlignWarpsSmall>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
+  const int    blocks = (nWarps + kAlignWarpsSmall - 1) / kAlignWarpsSmall;
+  const size_t smem   = align_smem_bytes(512);
+  cap.bandW           = 512;
+  auto k = extend_batch_kernel<512, kAlignWarpsSmall>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<blocks, kAlignWarpsSmall * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
   g_launches++;
-  } else {
-    auto k = extend_batch_kernel<8192, kAlignWarpsLarge>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<blocks, wpb * 32, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats);
-  g_launches++;
-  }
 }
 
-void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, u32 *keepCount,
-                      unsigned long long *keys, u32 *vals, cudaStream_t st) {
+void launch_extend_group(int threads, int U, int bandW, int ctas, ReadsDev R, DevParams P, const int *eml,
+                         const ExtendProblem *probs, u32 n, WarpScratch sc, AlignCaps cap, int *out, int *kind,
+                         int *deltaLen, u32 *status, unsigned long long *stats, cudaStream_t st) {
+  if (n == 0) return;
+  cap.bandW         = bandW;
+  const size_t smem = (size_t)2 * bandW * sizeof(int);
+  auto k = extend_group_kernel<false>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k<<<ctas, threads, smem, st>>>(R, P, eml, probs, n, sc, cap, out, kind, deltaLen, status, stats, U);
+  g_launches++;
+}
+
+void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
+                      const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys, u32 *vals,
+                      cudaStream_t st) {
   if (n == 0) return;
   unsigned g = (n + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
-  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, keepCount, keys, vals);
+  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, readLen, strRead, wideMinLen, binCount, keys, vals);
   g_launches++;
 }
 

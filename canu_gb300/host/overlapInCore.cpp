@@ -10,7 +10,12 @@
 //   * -l <n> (a per-read overlap cap that makes read pairs depend on each other) is
 //     rejected;
 //   * --gpu-device <d> picks the CUDA device, --ovb-snappy frames the records in snappy
-//     blocks as ovFile does (default: the six-word records unframed).
+//     blocks as ovFile does (default: the six-word records unframed);
+//   * --gpu-tune key=value[,key=value...] sets DP launch fields of oic_tuning
+//     (narrowArena, wideMinLen, wideThreads, wideTile, wideBandW, wideCtas, wideArena,
+//     forceWide), and --gpu-autotune <n> times the DP grid on the first n ref reads
+//     against the first hash block and keeps the fastest configuration (oic_autotune).
+//     Neither changes the records.
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -43,6 +48,7 @@ void usage(const char *prog) {
   fprintf(stderr, "  -partial -h a-b -H a-b -r a-b -R a-b -k <int|file> -m -u -z -t <n>\n");
   fprintf(stderr, "  --hashbits n --hashdatalen n --hashload f --maxerate f --alignnoise f\n");
   fprintf(stderr, "  --minlength n --minkmers -o out.ovb -s out.stats [--gpu-device d] [--ovb-snappy]\n");
+  fprintf(stderr, "  [--gpu-tune key=value,...] [--gpu-autotune nRefs]\n");
 }
 
 // Mark_Skip_Kmers file format (Build_Hash_Index.C:203-246): one k-mer per line (first
@@ -130,6 +136,32 @@ int writeOvb(const char *path, const std::vector<uint32_t> &rec, bool snappy) {
   return bad ? 1 : 0;
 }
 
+// --gpu-tune key=value[,key=value...] into an oic_tuning.
+bool parseTuning(const char *s, oic_tuning &t) {
+  std::string all = s;
+  size_t      p   = 0;
+  while (p <= all.size()) {
+    size_t      q   = all.find(',', p);
+    std::string kv  = all.substr(p, q == std::string::npos ? std::string::npos : q - p);
+    size_t      eq  = kv.find('=');
+    if (eq == std::string::npos) return false;
+    std::string k   = kv.substr(0, eq);
+    uint64_t    v   = strtoull(kv.c_str() + eq + 1, nullptr, 10);
+    if (k == "narrowArena") t.narrowArena = (uint32_t)v;
+    else if (k == "wideMinLen") t.wideMinLen = (uint32_t)v;
+    else if (k == "wideThreads") t.wideThreads = (uint32_t)v;
+    else if (k == "wideTile") t.wideTile = (uint32_t)v;
+    else if (k == "wideBandW") t.wideBandW = (uint32_t)v;
+    else if (k == "wideCtas") t.wideCtas = (uint32_t)v;
+    else if (k == "wideArena") t.wideArena = v;
+    else if (k == "forceWide") t.forceWide = (uint32_t)v;
+    else return false;
+    if (q == std::string::npos) break;
+    p = q + 1;
+  }
+  return true;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -138,7 +170,9 @@ int main(int argc, char **argv) {
   P.numThreads = 1;
   const char *store = nullptr, *outName = nullptr, *statName = nullptr, *skipFile = nullptr;
   int         device = 0, err = 0;
-  bool        snappy = false;
+  bool        snappy = false, haveTune = false;
+  oic_tuning  tune{};
+  uint32_t    autotuneRefs = 0;
 
   for (int a = 1; a < argc; a++) {
     const char *o   = argv[a];
@@ -178,6 +212,10 @@ int main(int argc, char **argv) {
     else if (!strcmp(o, "-z")) P.useHopelessCheck = 0;
     else if (!strcmp(o, "--gpu-device")) device = atoi(nxt());
     else if (!strcmp(o, "--ovb-snappy")) snappy = true;
+    else if (!strcmp(o, "--gpu-tune")) {
+      haveTune = true;
+      if (!parseTuning(nxt(), tune)) fprintf(stderr, "bad --gpu-tune value\n"), err++;
+    } else if (!strcmp(o, "--gpu-autotune")) autotuneRefs = (uint32_t)strtoul(nxt(), nullptr, 10);
     else if (!store) store = o;
     else {
       fprintf(stderr, "Unknown option '%s'\n", o);
@@ -215,6 +253,18 @@ int main(int argc, char **argv) {
     if (readSkipFile(skipFile, P.kmerLen, kmers)) return 1;
     rc = oic_set_skip_kmers(ctx, kmers.data(), kmers.size() / P.kmerLen);
     fprintf(stderr, "\nRead %zu kmers to mark to skip\n\n", kmers.size() / P.kmerLen);
+  }
+  if (!rc && haveTune) rc = oic_set_tuning(ctx, &tune);
+  if (!rc && autotuneRefs) {
+    // Tune on the first hash block and the first autotuneRefs ref reads of the -r range.
+    uint32_t last = 0;
+    rc = oic_load_hash_block(ctx, P.bgnHashID, P.endHashID, &last);
+    const uint32_t r0 = P.bgnRefID < 1 ? 1 : P.bgnRefID;
+    if (!rc) rc = oic_autotune(ctx, r0, r0 + autotuneRefs - 1, nullptr, 0, nullptr);
+    oic_tuning best;
+    if (!rc && !oic_get_tuning(ctx, &best))
+      fprintf(stderr, "autotune: wideThreads %u wideTile %u wideMinLen %u\n", best.wideThreads, best.wideTile,
+              best.wideMinLen);
   }
   if (!rc) rc = oic_run(ctx);
   if (rc) {
@@ -273,6 +323,9 @@ int main(int argc, char **argv) {
           (unsigned long)n, (unsigned long)st.seeds, (unsigned long)st.candidatePairs, (unsigned long)st.extensions,
           (unsigned long)st.dpCells, (unsigned long)st.dpCellsNoOverlap, (unsigned long)st.dpRows, st.msHash,
           st.msSeed, st.msAlign, st.msTotal);
+  fprintf(stderr, "GPU DP bins: one-warp %lu pairs %.2f ms; CTA %lu pairs (incl. reruns) %lu cells %.2f ms\n",
+          (unsigned long)st.pairsNarrow, st.msNarrow, (unsigned long)st.pairsWide, (unsigned long)st.cellsWide,
+          st.msWide);
   fprintf(stderr, "Bye.\n");
   oic_seqdb_free(&db);
   return 0;

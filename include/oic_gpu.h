@@ -70,6 +70,9 @@ typedef struct oic_stats {
   uint64_t dpCellsNoOverlap;                       /* DP cells spent on pairs that emitted nothing */
   uint64_t filteredPairs;                          /* candidate pairs the learned filter dropped */
   double   msFilter;                               /* device time of features + filter inference */
+  double   msNarrow, msWide;                       /* device time of the one-warp and CTA DP bins */
+  uint64_t pairsNarrow, pairsWide;                 /* pairs run in each bin (reruns in the CTA bin) */
+  uint64_t cellsWide;                              /* DP cells of the CTA bin */
 } oic_stats;
 
 typedef struct oic_ctx oic_ctx;
@@ -227,6 +230,48 @@ int oic_mlp_backward(const uint16_t *dParams, const uint16_t *dX, const uint16_t
                      uint16_t *dG1, uint16_t *dG2, float *dLoss, void *stream);
 int oic_mlp_adam(float *dMaster, float *dM, float *dV, float *dGrad, uint16_t *dParams, float lr, float beta1,
                  float beta2, float eps, float gradScale, float weightDecay, uint32_t step, void *stream);
+
+/* ---------------------------------------------------------------------------------
+ * DP launch configuration.  No counterpart in the reference (its DP runs one pair per
+ * OpenMP thread).  Candidate pairs go to one of two bins:
+ *   one-warp bin   one warp per pair, 8 warps per CTA, 512-int shared-memory rows
+ *                  (wider bands continue in HBM rows up to 16384), at most narrowArena
+ *                  kept DP cells per extension;
+ *   CTA bin        one pair per CTA of wideThreads threads (32 x warps per pair); each
+ *                  error row is computed by the whole CTA, wideTile diagonals per
+ *                  thread per pass (tile width 32 x wideTile per warp), wideBandW-int
+ *                  shared-memory rows, wideCtas CTAs, wideArena kept cells per CTA.
+ * A pair whose shorter read has at least wideMinLen bases (the length-bin boundary)
+ * goes straight to the CTA bin; a one-warp pair that exceeds a one-warp capacity is
+ * discarded without side effects and rerun in the CTA bin; a CTA-bin pair that
+ * exceeds its capacity is rerun on 8 CTAs holding the rest of the free memory.  Every
+ * configuration computes the same records; only the speed changes.  Zero fields take
+ * the defaults; oic_autotune() measures a grid and keeps the fastest. */
+typedef struct oic_tuning {
+  uint32_t narrowArena;   /* kept DP cells per extension in the one-warp bin (default 1 << 20) */
+  uint32_t wideMinLen;    /* length-bin boundary, bases of the shorter read (default: none) */
+  uint32_t wideThreads;   /* threads per CTA of the CTA bin: 64 .. 512, a multiple of 32 (default 256) */
+  uint32_t wideTile;      /* diagonals per thread per pass in the CTA bin: 1, 2 or 4 (default 1) */
+  uint32_t wideBandW;     /* shared-memory row width of the CTA bin, ints (default 12288) */
+  uint32_t wideCtas;      /* CTAs of the CTA bin (default: 2 per SM) */
+  uint64_t wideArena;     /* kept DP cells per CTA of the CTA bin (default: 2^24, less if memory is short) */
+  uint32_t forceWide;     /* testing: every pair goes to the CTA bin (0 / 1) */
+  uint32_t reserved;
+} oic_tuning;
+
+int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t);   /* NULL: defaults */
+int oic_get_tuning(oic_ctx *ctx, oic_tuning *t);          /* the configuration in use */
+
+/* Autotuner: runs the seed pass for ref reads [bgnRefID, endRefID] against the loaded
+ * hash block once, then times the DP of those candidate pairs under each configuration
+ * of a grid -- wideTile {1, 2, 4} x warps per pair {1 (one-warp bin only), 2, 4, 8} x
+ * length-bin boundary {none, 4 quantiles of the pairs' shorter read} -- checks that
+ * every configuration emits the same records, and sets the fastest.  With report
+ * non-NULL, fills report[0 .. maxReport) with one line per configuration:
+ * (wideTile, wideThreads, wideMinLen, narrow ms, wide ms, total ms, narrow cells,
+ * wide cells) as doubles, and *nReport with the number of lines. */
+int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *report, uint32_t maxReport,
+                 uint32_t *nReport);
 
 /* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
  * min(n, table length) entries; *len gets the table length. */

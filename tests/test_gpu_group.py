@@ -1,0 +1,96 @@
+"""The CTA-bin DP (several warps per read pair, U diagonals per thread) and the
+autotuner: same alignments as the oracle, same records as the reference."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import canu_gb300 as oic
+from conftest import golden_cases, golden_inputs, load_golden, run_cli  # noqa: F401
+from test_gpu_extend import make_problems, port_aligner
+
+pytestmark = pytest.mark.gpu
+
+SMALL_ARENA = 1 << 22   # keeps the tests' CTA-bin scratch small
+
+
+@pytest.mark.parametrize("threads,tile", [(64, 1), (128, 2), (256, 4), (512, 1)])
+@pytest.mark.parametrize("case,erate,partial", [("default", 0.06, 0), ("hierr", 0.12, 0), ("hierr_partial", 0.12, 1)])
+def test_cta_dp_matches_oracle(threads, tile, case, erate, partial, built, oracle, golden_inputs):
+    rng = np.random.default_rng(11)
+    db = golden_inputs[case]["db"]
+    seqs, probs = make_problems(db, 200, rng)
+    erate = float(np.float32(erate))
+    with oic.Overlapper(oic.default_params(kmerLen=22, maxErate=erate, partial=partial)) as ov:
+        ov.set_reads_seqdb(db)
+        ov.set_tuning(forceWide=1, wideThreads=threads, wideTile=tile, wideArena=SMALL_ARENA, wideCtas=64)
+        assert ov.tuning()["wideThreads"] == threads
+        a = np.array(probs, dtype=np.int64)
+        out, kind, dl = ov.extend_batch(a[:, 0] + 1, a[:, 1], a[:, 2] + 1, a[:, 3], a[:, 4], a[:, 5])
+    plib = ctypes.CDLL(oracle["lib"])
+    al = port_aligner(plib, erate, 1.0, partial)
+    comp = bytes.maketrans(b"acgtn", b"tgcan")
+    for i, (si, rev, t, ms, mo, ml) in enumerate(probs):
+        S = seqs[si] if not rev else seqs[si][::-1].translate(comp)
+        T = seqs[t]
+        o = np.zeros(5, dtype=np.int32)
+        dlen = ctypes.c_int32()
+        k = plib.oic_port_extend(al, S, len(S), T, len(T), ms, mo, ml, o.ctypes.data, None, ctypes.byref(dlen), None,
+                                 None)
+        assert k == kind[i] and (o == out[i]).all() and dlen.value == dl[i], (i, probs[i], k, o, kind[i], out[i])
+    plib.oic_port_aligner_free(al)
+
+
+@pytest.mark.parametrize("name", sorted(golden_cases()))
+def test_cta_bin_matches_reference(name, built, golden_inputs, tmp_path):
+    """Every pair through the CTA bin: records, .oc and stats equal the reference's."""
+    g = golden_inputs[name]
+    tune = f"forceWide=1,wideThreads=128,wideTile=2,wideArena={SMALL_ARENA},wideCtas=64"
+    rec, oc, st, log = run_cli(built["cli"], g["args"], g["db"], g["skip"], str(tmp_path), extra=["--gpu-tune", tune])
+    grec, goc, gst = load_golden(name)
+    assert rec.shape == grec.shape, log[-2000:]
+    assert (rec == grec).all()
+    assert oc == goc
+    assert st == gst
+
+
+def test_length_bin_and_small_one_warp_arena_keep_records(built, golden_inputs, tmp_path):
+    """A length-bin boundary inside the read-length range and a one-warp arena small
+    enough to overflow move pairs between bins without changing a record."""
+    name = "hierr"
+    g = golden_inputs[name]
+    tune = f"wideMinLen=6000,narrowArena=65536,wideThreads=256,wideTile=4,wideArena={SMALL_ARENA},wideCtas=64"
+    rec, oc, st, log = run_cli(built["cli"], g["args"], g["db"], g["skip"], str(tmp_path), extra=["--gpu-tune", tune])
+    grec, goc, gst = load_golden(name)
+    assert (rec == grec).all() and oc == goc and st == gst
+    import re
+    m = re.search(r"CTA (\d+) pairs", log)
+    assert m and int(m.group(1)) > 0, log[-1000:]
+
+
+def test_autotune_reports_the_grid_and_keeps_records(built, golden_inputs):
+    g = golden_inputs["hierr"]
+    db = g["db"]
+    n = len(oic.read_seqdb(db)[1])
+    p = oic.default_params(kmerLen=22, maxErate=0.12, minOlapLen=500, hashBits=22)
+
+    def run(tuned):
+        with oic.Overlapper(p) as ov:
+            ov.set_reads_seqdb(db)
+            ov.set_tuning(wideArena=SMALL_ARENA, wideCtas=64)
+            lines = None
+            if tuned:
+                ov.load_hash_block(1, n)
+                lines = ov.autotune(1, min(n, 400))
+            ov.load_hash_block(1, n)
+            ov.run_refs(1, n)
+            return oic.sort_records(ov.overlaps()), lines, ov.tuning()
+
+    base, _, _ = run(False)
+    recs, lines, tun = run(True)
+    assert len(lines) == 16                      # 4 warps-per-pair x 3 tiles, then 4 length bins
+    assert {(l["wideThreads"], l["wideTile"]) for l in lines[:12]} == {(t, u) for t in (64, 128, 256, 512)
+                                                                        for u in (1, 2, 4)}
+    best = min(lines, key=lambda l: l["msTotal"])
+    assert tun["wideThreads"] == best["wideThreads"] and tun["wideTile"] == best["wideTile"]
+    assert np.array_equal(recs, base)
