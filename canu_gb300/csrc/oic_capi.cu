@@ -576,6 +576,14 @@ int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning
       if (verbose()) fprintf(stderr, "oic: %u pairs moved from the one-warp DP to the CTA DP\n", nOvf);
       CK(cudaMemcpyAsync(ctx->dWork.as<uint32_t>() + nNarrow + nWide, ctx->dAlnOvf.p, nOvf * sizeof(uint32_t),
                          cudaMemcpyDeviceToDevice, ctx->st));
+      // The moved pairs arrive in completion order: sort the whole CTA-bin list so the
+      // pairs with the most match nodes (the longest chains of extensions) start first.
+      uint32_t *lst = ctx->dWork.as<uint32_t>() + nNarrow;
+      launch_list_keys(ctx->dPairs.as<PairRec>(), lst, nW, ctx->dWorkK.as<u64>(), ctx->dWorkV2.as<uint32_t>(),
+                       ctx->st);
+      CK(cudaMemcpyAsync(lst, ctx->dWorkV2.p, (size_t)nW * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->st));
+      CK(radix_sort_u64_u32(ctx->dWorkK.as<u64>(), lst, ctx->dWorkK2.as<u64>(), ctx->dWorkV2.as<uint32_t>(), nW, 32,
+                            ctx->dWorkScratch.p, ctx->st));
     }
     for (int level = 0; level < 2 && nW; level++) {
       const bool huge = level == 1;

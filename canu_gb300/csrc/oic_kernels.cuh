@@ -142,6 +142,10 @@ void launch_pair_features(const PairRec *pairs, u32 n, const int4 *nodes, const 
 cudaError_t launch_mlp_forward(const void *prm, const void *X, u32 n, float *logit, void *H1, void *H2,
                                cudaStream_t st);
 
+// Sort keys of a list of pair indices: the pairs with the most match nodes first.
+void launch_list_keys(const PairRec *pairs, const u32 *list, u32 n, unsigned long long *keys, u32 *vals,
+                      cudaStream_t st);
+
 // Compact per-pair record slots into a dense record array.
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st);
 

@@ -552,6 +552,17 @@ __global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit
   }
 }
 
+// keys[i] = 2^30 - 1 - match nodes of pair list[i], vals[i] = list[i]: the order that
+// puts a list's pairs with the most match nodes first.
+__global__ void list_keys_kernel(const PairRec *pairs, const u32 *list, u32 n, unsigned long long *keys, u32 *vals) {
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const u32 pi = list[i];
+    const u32 nc = pairs[pi].nodeCnt < 0x3fffffffu ? pairs[pi].nodeCnt : 0x3fffffffu;
+    keys[i]      = 0x3fffffffu - nc;
+    vals[i]      = pi;
+  }
+}
+
 __global__ void compact_records_kernel(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst) {
   for (u32 p = blockIdx.x * blockDim.x + threadIdx.x; p < nPairs; p += gridDim.x * blockDim.x) {
     const u32 c = cnt[p];
@@ -622,6 +633,15 @@ void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float log
   unsigned g = (n + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
   work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, readLen, strRead, wideMinLen, binCount, keys, vals);
+  g_launches++;
+}
+
+void launch_list_keys(const PairRec *pairs, const u32 *list, u32 n, unsigned long long *keys, u32 *vals,
+                      cudaStream_t st) {
+  if (n == 0) return;
+  unsigned g = (n + 255) / 256;
+  if (g > 65535u * 8) g = 65535u * 8;
+  list_keys_kernel<<<g, 256, 0, st>>>(pairs, list, n, keys, vals);
   g_launches++;
 }
 
