@@ -346,7 +346,7 @@ def main():
     if a.workload == "c2" and os.path.exists(fpath) and not a.no_filter:
         from canu_gb300 import filter_train
         fprm, fthr, ffull, fmeta = filter_train.load(fpath)
-        ov.set_filter(fprm, fthr, ffull)
+        ov.set_filter(fprm, fthr, ffull, fmeta.get("budget", 1))
         fres, _, frec = timed(False)
         ov.set_filter(None, 0.0)
         recall, exact = filter_train.compare(plain_rec, frec)
@@ -361,7 +361,8 @@ def main():
                 "recall_vs_plain": recall, "records_identical_to_plain": exact,
                 "dp_cells": fst["dpCells"], "dp_cells_skipped_frac": None, "filtered_pairs": fst["filteredPairs"],
                 "ms_filter": fst["msFilter"], "ms_align": fst["msAlign"],
-                "thresholds": {"drop_below_p": fthr, "single_extension_below_p": ffull},
+                "thresholds": {"drop_below_p": fthr, "budget_tier_below_p": ffull,
+                               "extension_budget": fmeta.get("budget", 1)},
                 "trained_on": f"c2 seeds {fmeta.get('train_seeds')}; this read set is seed "
                               f"{workloads.WORKLOADS[a.workload]['synth']['seed']} (held out)",
                 "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in fres))}

@@ -122,7 +122,7 @@ def library():
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
-        lib.oic_set_filter.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float]
+        lib.oic_set_filter.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float, U32]
         lib.oic_collect_pairs.argtypes = [vp, ctypes.c_int]
         lib.oic_num_pairs.argtypes = [vp, P(U64), P(U64)]
         lib.oic_get_pairs.argtypes = [vp, vp, vp, vp, U64, U64]
@@ -267,17 +267,18 @@ class Overlapper:
         self._check(self._lib.oic_get_match_limit(self._ctx, _ptr(out), n.value, ctypes.byref(n)))
         return out
 
-    def set_filter(self, params, threshold, full_threshold=0.0):
+    def set_filter(self, params, threshold, full_threshold=0.0, ext_budget=1):
         """Learned candidate filter: params = FILTER_NPARAM float16 values (None: off).
-        Pairs scored below threshold are dropped; below full_threshold they stop after a
-        first extension that found no overlap."""
+        Pairs scored below threshold are dropped; below full_threshold they stop once
+        ext_budget extensions have found no overlap."""
         if params is None:
-            self._check(self._lib.oic_set_filter(self._ctx, None, 0.0, 0.0))
+            self._check(self._lib.oic_set_filter(self._ctx, None, 0.0, 0.0, 0))
             return
         prm = np.ascontiguousarray(params, dtype=np.float16).view(np.uint16)
         if prm.size != FILTER_NPARAM:
             raise ValueError(f"filter needs {FILTER_NPARAM} parameters, got {prm.size}")
-        self._check(self._lib.oic_set_filter(self._ctx, _ptr(prm), float(threshold), float(full_threshold)))
+        self._check(self._lib.oic_set_filter(self._ctx, _ptr(prm), float(threshold), float(full_threshold),
+                                             int(ext_budget)))
 
     def collect_pairs(self, mode=1):
         """0 off, 1 candidate pairs + feature rows, 2 also their match runs."""

@@ -140,6 +140,10 @@ struct oic_ctx {
   DevBuf dSeedSlotK, dSeedSlotV, dSeedPairs, dSeedNodes;        // normal configuration
   DevBuf dSeedSlotK2, dSeedSlotV2, dSeedPairs2, dSeedNodes2;    // wide configuration
   uint32_t pairCap = 0, nodeCap = 0;
+  // Candidate pairs and match runs per (ref read x block string) of the batches so far,
+  // to size the next batch; the demand of the last batch that did not fit.
+  double   pairDensity = 0, nodeDensity = 0;
+  uint64_t overPairs = 0, overNodes = 0;
 
   // align
   DevBuf dWork, dRec, dCnt, dRecPos, dRecOut, dAlnOvf, dWorkK, dWorkK2, dWorkV2, dWorkScratch;
@@ -153,7 +157,8 @@ struct oic_ctx {
   // learned candidate filter
   bool   filterOn       = false;
   float  filterLogitThr = 0.0f;      // drop below
-  float  filterTierThr  = -INFINITY; // single-extension tier below
+  float  filterTierThr  = -INFINITY; // extension-budget tier below
+  int    filterBudget   = 1;         // extensions without an overlap allowed in that tier
   DevBuf dFilterPrm, dFeat, dLogit, dPairCells, dPairExt;
   cudaEvent_t evF0 = nullptr, evF1 = nullptr;
   int    collect = 0;                      // 0 off, 1 pairs + features, 2 also match runs
@@ -430,7 +435,13 @@ int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t e
   uint32_t h[16];
   CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
   if ((rc = sync_check(ctx, "seed kernel"))) return rc;
-  if (h[cErr] & (kErrOutNodes | kErrOutPairs)) return kRetrySmaller;
+  if (h[cErr] & (kErrOutNodes | kErrOutPairs)) {
+    // Every segment reserved its output with one atomic add, so the counters hold the
+    // batch's whole demand.
+    ctx->overPairs = h[cPairCount];
+    ctx->overNodes = h[cNodeCount];
+    return kRetrySmaller;
+  }
   if (h[cSegOvf] > 0) {
     // Segments whose pair table or node pool overflowed run again in the wide
     // configuration; their ids are the work list of that pass.
@@ -447,7 +458,11 @@ int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t e
                 ctr32(ctx) + cSegCounter, ssw, sw.caps, sw.warps, so, ctx->st);
     CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
     if ((rc = sync_check(ctx, "seed kernel (wide)"))) return rc;
-    if (h[cErr] & (kErrOutNodes | kErrOutPairs)) return kRetrySmaller;
+    if (h[cErr] & (kErrOutNodes | kErrOutPairs)) {
+      ctx->overPairs = h[cPairCount];
+      ctx->overNodes = h[cNodeCount];
+      return kRetrySmaller;
+    }
     if (h[cSegOvf] > 0)
       return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
   }
@@ -536,6 +551,7 @@ int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning
   const bool tier  = useFilter && ctx->filterTierThr > ctx->filterLogitThr;
   ao.tierLogit     = tier ? ctx->dLogit.as<float>() : nullptr;
   ao.tierThr       = ctx->filterTierThr;
+  ao.tierBudget    = ctx->filterBudget;
 
   cudaEvent_t ev[4];
   for (auto &x : ev) CK(cudaEventCreate(&x));
@@ -1153,8 +1169,19 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
   cudaEventCreate(&e2);
   float msSeed = 0, msAlign = 0;
   size_t   pos   = 0;
-  uint32_t batch = (uint32_t)refs.size();
   int      rc    = OIC_OK;
+  // Batch size from the density of earlier batches (any block, scaled by this block's
+  // string count), else from 256 candidate pairs and 4096 match runs per ref read;
+  // 20 % headroom.
+  const double strs = std::max<double>(1.0, ctx->blkN);
+  auto size_for = [&](double pairsPerRef, double nodesPerRef) {
+    double lim = (double)refs.size();
+    if (pairsPerRef > 0) lim = std::min(lim, 0.8 * ctx->pairCap / pairsPerRef);
+    if (nodesPerRef > 0) lim = std::min(lim, 0.8 * ctx->nodeCap / nodesPerRef);
+    return (uint32_t)std::max(1.0, lim);
+  };
+  uint32_t batch = ctx->pairDensity > 0 ? size_for(ctx->pairDensity * strs, ctx->nodeDensity * strs)
+                                        : size_for(256.0, 4096.0);
   while (pos < refs.size()) {
     const uint32_t nb = (uint32_t)std::min<size_t>(batch, refs.size() - pos);
     const size_t   outMark = ctx->out.size();
@@ -1163,19 +1190,18 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
     if (rc == kRetrySmaller && nb > 1) {
       ctx->out.resize(outMark);
       ctx->stats = saved;
-      batch      = (nb + 1) / 2;
+      // The failed batch's demand sizes the retry (at most half the failed size).
+      batch = std::min<uint32_t>((nb + 1) / 2, size_for((double)ctx->overPairs / nb, (double)ctx->overNodes / nb));
       if (verbose()) fprintf(stderr, "oic: batch output full, retrying with %u ref reads per batch\n", batch);
       continue;
     }
     if (rc) break;
     pos += nb;
-    // Size the next batch from the pair and node density seen so far (25% headroom).
     const double pr = (double)(ctx->stats.candidatePairs - saved.candidatePairs) / nb;
     const double nr = (double)(ctx->stats.nodes - saved.nodes) / nb;
-    double lim = (double)refs.size();
-    if (pr > 0) lim = std::min(lim, 0.8 * ctx->pairCap / pr);
-    if (nr > 0) lim = std::min(lim, 0.8 * ctx->nodeCap / nr);
-    batch = (uint32_t)std::max(1.0, std::min(lim, (double)refs.size()));
+    ctx->pairDensity = std::max(ctx->pairDensity, pr / strs);
+    ctx->nodeDensity = std::max(ctx->nodeDensity, nr / strs);
+    batch            = size_for(std::max(pr, ctx->pairDensity * strs), std::max(nr, ctx->nodeDensity * strs));
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1264,7 +1290,7 @@ int oic_get_stats(oic_ctx *ctx, oic_stats *st) {
   return OIC_OK;
 }
 
-int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold) {
+int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold, uint32_t extBudget) {
   if (!ctx) return OIC_ERR_ARG;
   if (!params) {
     ctx->filterOn = false;
@@ -1284,6 +1310,7 @@ int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float 
   };
   ctx->filterLogitThr = logit(threshold);
   ctx->filterTierThr  = logit(fullThreshold);
+  ctx->filterBudget   = extBudget ? (int)extBudget : 1;
   ctx->filterOn       = true;
   return OIC_OK;
 }

@@ -92,8 +92,9 @@ struct AlignOut {
   u32 *cells;           // optional: DP cells spent on each pair slot (saturating) ...
   int4 *ext;            // ... and (extensions, first extension with an overlap or -1,
                         //      cells of the first extension, extension limit applied)
-  const float *tierLogit;   // optional: pairs scored below tierThr stop after their first
-  float        tierThr;     // extension when it found no overlap
+  const float *tierLogit;   // optional: pairs scored below tierThr stop once tierBudget
+  float        tierThr;     // extensions have run without finding an overlap
+  int          tierBudget;
 };
 
 enum StatIdx {

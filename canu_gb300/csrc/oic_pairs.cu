@@ -440,7 +440,7 @@ static __device__ __forceinline__ void align_loop(WarpDP &w, PairSmem &ps, const
     w.err = 0;
     const unsigned long long cellsBefore = w.cells;
     int extLimit = 0;   // 0: every match node may be extended (the reference's rule)
-    if (out.tierLogit && out.tierLogit[pi] < out.tierThr) extLimit = 1;
+    if (out.tierLogit && out.tierLogit[pi] < out.tierThr) extLimit = out.tierBudget;
     const bool ok = process_pair<GROUP>(w, ps, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, extLimit);
     if (lane == 0) {
       if (ok) {

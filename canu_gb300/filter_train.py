@@ -50,7 +50,8 @@ def init_params(seed=0):
     return p.astype(np.float16)
 
 
-def run_workload(name, seed, scale, workdir, device=0, collect=0, params=None, threshold=0.0, full_threshold=0.0):
+def run_workload(name, seed, scale, workdir, device=0, collect=0, params=None, threshold=0.0, full_threshold=0.0,
+                 ext_budget=1):
     """One whole job of a workload: (records, stats, pairs info, feature rows)."""
     db, skip = workloads.generate(name, workdir, scale=scale, seed=seed)
     with Overlapper(workloads.params(name), device) as ov:
@@ -58,7 +59,7 @@ def run_workload(name, seed, scale, workdir, device=0, collect=0, params=None, t
         if skip:
             ov.set_skip_kmers(workloads.read_skip(skip))
         if params is not None:
-            ov.set_filter(params, threshold, full_threshold)
+            ov.set_filter(params, threshold, full_threshold, ext_budget)
         if collect:
             ov.collect_pairs(collect)
         ov.run()
@@ -168,26 +169,31 @@ def _logit(p):
     return -np.inf if p <= 0 else math.log(p / (1 - p))
 
 
-def policy_cost(info, logit, t_drop, t_full):
+def policy_cost(info, logit, t_drop, t_full, budget=1):
     """(recall, DP cells, pairs kept) of the two-threshold policy replayed on collected
     pairs: dropped pairs cost nothing and lose their overlaps; pairs below t_full stop
-    after a first extension that found nothing, so they lose the overlaps a later
-    extension would have found (firstHit > 0) and cost only cellsFirst."""
+    once `budget` extensions found nothing, so they lose the overlaps found later
+    (firstHit >= budget) and cost their first extension plus, for budget > 1, the mean
+    cost of their later extensions times the extra ones run."""
     y = info["overlaps"] > 0
     fh = info["firstHit"]
     cells = info["cells"].astype(np.float64)
     first = info["cellsFirst"].astype(np.float64)
+    ext = info["extensions"].astype(np.float64)
     z = np.asarray(logit, dtype=np.float32)
     keep = ~(z < np.float32(_logit(t_drop)))
     single = keep & (z < np.float32(_logit(t_full)))
-    cost = np.where(single & ~(y & (fh == 0)), first, cells)[keep].sum()
-    lost = (y & ~keep).sum() + (single & y & (fh > 0)).sum()
+    later = (cells - first) / np.maximum(ext - 1, 1)
+    capped = first + np.maximum(np.minimum(ext, budget) - 1, 0) * later
+    found_early = y & (fh >= 0) & (fh < budget)
+    cost = np.where(single & ~found_early, capped, cells)[keep].sum()
+    lost = (y & ~keep).sum() + (single & y & (fh >= budget)).sum()
     return 1.0 - lost / max(y.sum(), 1), float(cost), int(keep.sum())
 
 
-def choose_thresholds(info, logit, recall_drop, recall_total):
+def choose_thresholds(info, logit, recall_drop, recall_total, budget=1):
     """t_drop keeps recall_drop of the positives; t_full is the lowest cut (the most
-    pairs on a single extension) whose replayed recall still reaches recall_total."""
+    pairs on the extension budget) whose replayed recall still reaches recall_total."""
     y = info["overlaps"] > 0
     t_drop = choose_threshold(logit, y, recall_drop)
     z = np.asarray(logit, dtype=np.float64)
@@ -198,10 +204,10 @@ def choose_thresholds(info, logit, recall_drop, recall_total):
         t_full = 0.0 if q == 0.0 else (1.0 if not np.isfinite(zc) else float(1 / (1 + math.exp(-zc))))
         if t_full >= 1.0:
             t_full = 0.999999
-        rec, cost, _ = policy_cost(info, logit, t_drop, t_full if q > 0 else t_drop)
+        rec, cost, _ = policy_cost(info, logit, t_drop, t_full if q > 0 else t_drop, budget)
         if rec >= recall_total and (best is None or cost < best[1]):
             best = (t_full if q > 0 else t_drop, cost, rec)
-    if best is None:   # the single-extension tier costs too much recall: full for every kept pair
+    if best is None:   # the budget tier costs too much recall: full extension for every kept pair
         return t_drop, t_drop
     return t_drop, best[0]
 
@@ -228,31 +234,36 @@ def compare(plain, filt):
 
 
 def evaluate(params, threshold, name="c2", seed=6, scale=1.0, workdir="/tmp/oic_filter", device=0,
-             full_threshold=None):
-    """Plain vs filtered run of one read set; returns a dict of the measured figures."""
+             full_threshold=None, budget=1, pairs=True):
+    """Plain vs filtered run of one read set; returns a dict of the measured figures.
+    pairs=False skips the pair-level figures (a third run collecting every pair)."""
     if full_threshold is None:
         full_threshold = threshold
-    _, _, info, _ = run_workload(name, seed, scale, workdir, device, collect=1, params=params, threshold=0.0)
-    y = info["overlaps"] > 0
-    rec_replay, _, kept = policy_cost(info, info["score"], threshold, full_threshold)
-    keep = ~(info["score"] < np.float32(_logit(threshold)))
+    out = {}
+    if pairs:
+        _, _, info, _ = run_workload(name, seed, scale, workdir, device, collect=1, params=params, threshold=0.0)
+        y = info["overlaps"] > 0
+        rec_replay, _, kept = policy_cost(info, info["score"], threshold, full_threshold, budget)
+        keep = ~(info["score"] < np.float32(_logit(threshold)))
+        cells_neg = info["cells"][~y].astype(np.float64)
+        out = {"pairs": int(len(info)), "positives": int(y.sum()), "kept": int(keep.sum()),
+               "pair_recall_drop_only": float((keep & y).sum() / max(y.sum(), 1)),
+               "precision": float((keep & y).sum() / max(keep.sum(), 1)),
+               "recall_replayed": float(rec_replay),
+               "dropped_negative_cells_frac": float(cells_neg[~keep[~y]].sum() / max(cells_neg.sum(), 1))}
+        del info
     rp, sp, _, _ = run_workload(name, seed, scale, workdir, device)
     rf, sf, _, _ = run_workload(name, seed, scale, workdir, device, params=params, threshold=threshold,
-                                full_threshold=full_threshold)
+                                full_threshold=full_threshold, ext_budget=budget)
     recall, exact = compare(rp, rf)
-    cells_neg = info["cells"][~y].astype(np.float64)
     mk = lambda recs, s: {
         "overlaps": int(len(recs)), "ms": s["msTotal"], "ms_align": s["msAlign"], "dp_cells": int(s["dpCells"]),
         "overlaps_per_s": len(recs) / (s["msTotal"] / 1e3), "dp_cells_per_s": s["dpCells"] / (s["msTotal"] / 1e3)}
     f = mk(rf, sf)
     f.update({"ms_filter": sf["msFilter"], "filtered_pairs": int(sf["filteredPairs"])})
     return {
-        "pairs": int(len(info)), "positives": int(y.sum()), "kept": int(keep.sum()),
-        "pair_recall_drop_only": float((keep & y).sum() / max(y.sum(), 1)),
-        "precision": float((keep & y).sum() / max(keep.sum(), 1)),
-        "recall_replayed": float(rec_replay),
-        "dropped_negative_cells_frac": float(cells_neg[~keep[~y]].sum() / max(cells_neg.sum(), 1)),
-        "thresholds": {"drop": threshold, "full": full_threshold},
+        **out,
+        "thresholds": {"drop": threshold, "full": full_threshold, "budget": budget},
         "plain": mk(rp, sp), "filter": f,
         "recall": recall, "records_exact": bool(exact),
         "dp_cells_skipped_frac": 1.0 - sf["dpCells"] / max(sp["dpCells"], 1),
@@ -260,16 +271,18 @@ def evaluate(params, threshold, name="c2", seed=6, scale=1.0, workdir="/tmp/oic_
     }
 
 
-def save(path, params, threshold, full_threshold, meta):
+def save(path, params, threshold, full_threshold, meta, budget=1):
     np.savez(path, params=np.asarray(params, dtype=np.float16), threshold=np.float64(threshold),
-             full_threshold=np.float64(full_threshold), meta=np.array(json.dumps(meta)))
+             full_threshold=np.float64(full_threshold), budget=np.int64(budget), meta=np.array(json.dumps(meta)))
 
 
 def load(path):
-    """(params float16[FILTER_NPARAM], drop threshold, full threshold, meta dict)."""
+    """(params float16[FILTER_NPARAM], drop threshold, full threshold, meta dict); the
+    extension budget is meta["budget"]."""
     z = np.load(path)
-    return (z["params"].astype(np.float16), float(z["threshold"]), float(z["full_threshold"]),
-            json.loads(str(z["meta"])))
+    meta = json.loads(str(z["meta"]))
+    meta["budget"] = int(z["budget"]) if "budget" in z else 1
+    return z["params"].astype(np.float16), float(z["threshold"]), float(z["full_threshold"]), meta
 
 
 def main(argv=None):
@@ -281,13 +294,15 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--batch", type=int, default=32768)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--recall-drop", type=float, default=0.9996)
-    ap.add_argument("--recall", type=float, default=0.9993)
+    ap.add_argument("--recall-drop", type=float, default=0.99998)
+    ap.add_argument("--recall", type=float, default=0.9995)
+    ap.add_argument("--budget", type=int, default=2, help="extensions without an overlap in the budget tier")
     ap.add_argument("--pos-weight", type=float, default=4.0)
     ap.add_argument("--init-seed", type=int, default=0)
     ap.add_argument("--workdir", default="/tmp/oic_filter")
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--also-eval", default="", help="more read sets to evaluate on, e.g. c5:5 (workload:seed)")
     a = ap.parse_args(argv)
     import torch
 
@@ -324,8 +339,8 @@ def main(argv=None):
     logit = tr.predict(X).cpu().numpy()
     yl = y.cpu().numpy()
     info = np.concatenate(info_all)
-    thr, full = choose_thresholds(info, logit, a.recall_drop, a.recall)
-    rec_tr, cost_tr, kept_tr = policy_cost(info, logit, thr, full)
+    thr, full = choose_thresholds(info, logit, a.recall_drop, a.recall, a.budget)
+    rec_tr, cost_tr, kept_tr = policy_cost(info, logit, thr, full, a.budget)
     params = tr.params()
     meta = {"workload": a.workload, "scale": a.scale, "train_seeds": a.train_seeds, "epochs": a.epochs,
             "batch": a.batch, "lr": a.lr, "recall_drop_train": a.recall_drop, "recall_target_train": a.recall,
@@ -333,20 +348,26 @@ def main(argv=None):
             "train_seconds": train_s, "train_samples_per_s": n * a.epochs / train_s,
             "train_tflops": flops / train_s / 1e12, "train_recall_replayed": rec_tr,
             "train_cells_left_frac": cost_tr / float(info["cells"].astype(np.float64).sum()),
-            "train_pairs_kept": kept_tr}
+            "train_pairs_kept": kept_tr, "budget": a.budget}
     log(f"thresholds: drop {thr:.6g}, full {full:.6g}; training replay: recall {rec_tr:.5f}, "
         f"cells left {meta['train_cells_left_frac']:.4f}, pairs kept {kept_tr}")
     if a.out:
-        save(a.out, params, thr, full, meta)
+        save(a.out, params, thr, full, meta, a.budget)
         log(f"wrote {a.out}")
     del X, y, w
     torch.cuda.empty_cache()
-    ev = evaluate(params, thr, a.workload, a.eval_seed, a.scale, a.workdir, full_threshold=full)
+    ev = evaluate(params, thr, a.workload, a.eval_seed, a.scale, a.workdir, full_threshold=full, budget=a.budget)
     log(json.dumps(ev))
+    more = {}
+    for spec in [s for s in a.also_eval.split(",") if s]:
+        wl, sd = spec.split(":")
+        more[spec] = evaluate(params, thr, wl, int(sd), 1.0, a.workdir, full_threshold=full, budget=a.budget,
+                              pairs=False)
+        log(spec + " " + json.dumps(more[spec]))
     if a.report:
         with open(a.report, "w") as f:
-            json.dump({"meta": meta, "threshold": thr, "full_threshold": full, "eval_seed": a.eval_seed,
-                       "eval": ev}, f, indent=1)
+            json.dump({"meta": meta, "threshold": thr, "full_threshold": full, "budget": a.budget,
+                       "eval_seed": a.eval_seed, "eval": ev, "also": more}, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -97,6 +97,7 @@ def _fake_pairs():
     info["firstHit"] = [0, 0, 0, -1, -1, -1, -1, 2]
     info["cells"] = [100, 100, 100, 1000, 1000, 50, 0, 300]
     info["cellsFirst"] = [100, 100, 100, 70, 70, 50, 0, 60]
+    info["extensions"] = [1, 1, 1, 10, 10, 1, 0, 3]
     logit = np.array([3.0, 2.0, 1.0, 2.5, -1.0, -2.0, -3.0, 4.0], dtype=np.float32)
     return info, logit
 
@@ -116,6 +117,12 @@ def test_policy_replay_counts_dropped_and_single_extension_pairs():
     # full extension from 3.5 up keeps pair 7
     rec, cost, _ = filter_train.policy_cost(info, logit, sig(0.0), sig(3.5))
     assert rec == 1.0 and cost == 300 + 70 + 300
+    # a budget of 2: pair 7 (found by its third extension) is still lost; pair 3 pays
+    # one more extension at its mean later cost (930 / 9); a budget of 3 keeps pair 7
+    rec, cost, _ = filter_train.policy_cost(info, logit, sig(0.0), sig(5.0), budget=2)
+    assert rec == 0.75 and abs(cost - (300 + 70 + 930 / 9 + 60 + 120)) < 1e-9
+    rec, cost, _ = filter_train.policy_cost(info, logit, sig(0.0), sig(5.0), budget=3)
+    assert rec == 1.0 and abs(cost - (300 + 70 + 2 * 930 / 9 + 300)) < 1e-9
 
 
 def test_threshold_pair_meets_the_training_recall():

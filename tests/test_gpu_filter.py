@@ -241,7 +241,8 @@ def test_trained_filter_gains_over_the_plain_path(small_c2):
     params, thr, full, meta = filter_train.load(path)
     assert "6" not in meta["train_seeds"].split(",")
     d, _ = small_c2
-    ev = filter_train.evaluate(params, thr, "c2", seed=6, scale=0.05, workdir=d, full_threshold=full)
+    ev = filter_train.evaluate(params, thr, "c2", seed=6, scale=0.05, workdir=d, full_threshold=full,
+                               budget=meta["budget"])
     assert ev["records_exact"]
     assert ev["recall"] >= 0.995
     assert ev["dp_cells_skipped_frac"] > 0.3
