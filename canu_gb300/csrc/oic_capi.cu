@@ -262,7 +262,7 @@ struct AlignConfig {
 AlignConfig align_normal(const oic_ctx *c) {
   AlignConfig a;
   a.bandW         = 512;
-  a.warps         = c->nSM * 3 * align_warps_per_block(512);
+  a.warps         = c->nSM * OIC_ALIGN_MIN_BLOCKS * align_warps_per_block(512);
   a.caps.arenaCap = 1 << 20;
   a.caps.rowCap   = 1 << 14;
   a.caps.nodeCap  = 1 << 16;
@@ -1528,6 +1528,7 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
     AlignTimes at;
   };
   std::vector<Line>     lines;
+  size_t                stage1 = 0;   // lines of stage 1 (no length bin)
   std::vector<uint32_t> ref0;
   bool                  haveRef = false;
   oic_tuning base       = resolved_tuning(ctx);
@@ -1567,6 +1568,7 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
       size_t best = 0;
       for (size_t i = 1; i < lines.size(); i++)
         if (total(lines[i]) < total(lines[best])) best = i;
+      stage1 = lines.size();
       const double qs[] = {0.5, 0.9, 0.99, 0.999};
       for (double q : qs) {
         oic_tuning t = lines[best].t;
@@ -1582,10 +1584,21 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
   ctx->out.resize(outMark);
   if (rc) return rc;
   if (!lines.empty()) {
+    // Best configuration without a length bin; a length bin is taken only when it is
+    // more than 5 % faster (a sample is dominated by its longest pairs, so smaller
+    // differences are noise).
+    if (!stage1) stage1 = lines.size();
     size_t best = 0;
-    for (size_t i = 1; i < lines.size(); i++)
+    for (size_t i = 1; i < stage1; i++)
       if (total(lines[i]) < total(lines[best])) best = i;
+    for (size_t i = stage1; i < lines.size(); i++)
+      if (total(lines[i]) < 0.95 * total(lines[best])) best = i;
     ctx->tune = lines[best].t;
+    if (verbose())
+      for (const Line &l : lines)
+        fprintf(stderr, "oic: autotune: threads %u tile %u length bin %d: one-warp %.1f ms, CTA %.1f ms\n",
+                l.t.wideThreads, l.t.wideTile, l.t.wideMinLen == 0xffffffffu ? -1 : (int)l.t.wideMinLen,
+                l.at.msNarrow, l.at.msWide);
     if (verbose())
       fprintf(stderr, "oic: autotune: %zu configurations on %u pairs; best: %u threads, tile %u, length bin %u (%.1f ms)\n",
               lines.size(), nPairs, ctx->tune.wideThreads, ctx->tune.wideTile, ctx->tune.wideMinLen,

@@ -8,6 +8,11 @@
 #include "oic_common.cuh"
 #include "oic_align.cuh"
 
+// CTAs of the one-warp DP kernel resident per SM (its register budget follows).
+#ifndef OIC_ALIGN_MIN_BLOCKS
+#define OIC_ALIGN_MIN_BLOCKS 3
+#endif
+
 namespace oic {
 
 // ---------------- reads ----------------

@@ -475,7 +475,7 @@ static __device__ __forceinline__ void align_loop(WarpDP &w, PairSmem &ps, const
 
 // One pair per warp, WARPS warps per CTA.
 template <int BANDW, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? 3 : 1)) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
+__global__ void __launch_bounds__(WARPS * 32, (WARPS > 1 ? OIC_ALIGN_MIN_BLOCKS : 1)) align_kernel(ReadsDev R, TableDev Tb, DevParams P, const int *eml,
                                                            const PairRec *pairs, const u32 *work, u32 nWork,
                                                            u32 *workCounter, const int4 *nodes, WarpScratch scBase,
                                                            AlignCaps cap, AlignOut out) {

@@ -195,12 +195,13 @@ typedef struct oic_pair_info {
 /* Set the filter (params: host array of OIC_FILTER_NPARAM FP16 bit patterns) and its
  * probability thresholds, p = sigmoid(logit):
  *   p <  dropThreshold                  the pair is not extended;
- *   dropThreshold <= p < fullThreshold  the pair stops after its first extension if
- *                                       that extension found no overlap;
+ *   dropThreshold <= p < fullThreshold  the pair stops once extBudget extensions (0
+ *                                       means 1) have run without finding an overlap;
  *   p >= fullThreshold                  every match is extended (the reference's rule).
  * fullThreshold <= dropThreshold disables the middle tier.  params NULL turns the
  * filter off. */
-int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float dropThreshold, float fullThreshold);
+int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float dropThreshold, float fullThreshold,
+                   uint32_t extBudget);
 
 /* Pair collection for training and evaluation: mode 0 off, 1 pairs and feature rows,
  * 2 also the match runs (T offset, length, S start per run).  Collected data accumulate
@@ -266,7 +267,9 @@ int oic_get_tuning(oic_ctx *ctx, oic_tuning *t);          /* the configuration i
  * hash block once, then times the DP of those candidate pairs under each configuration
  * of a grid -- wideTile {1, 2, 4} x warps per pair {1 (one-warp bin only), 2, 4, 8} x
  * length-bin boundary {none, 4 quantiles of the pairs' shorter read} -- checks that
- * every configuration emits the same records, and sets the fastest.  With report
+ * every configuration emits the same records, and sets the fastest (a length bin only
+ * when it beats the best configuration without one by more than 5 %).  The sample's
+ * DP runs once per configuration (16 times): keep it to a few seconds of DP.  With report
  * non-NULL, fills report[0 .. maxReport) with one line per configuration:
  * (wideTile, wideThreads, wideMinLen, narrow ms, wide ms, total ms, narrow cells,
  * wide cells) as doubles, and *nReport with the number of lines. */
