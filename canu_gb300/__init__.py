@@ -79,7 +79,7 @@ class OicStats(ctypes.Structure):
         ("msReads", ctypes.c_double), ("kernelLaunches", ctypes.c_uint64), ("dpCellsNoOverlap", ctypes.c_uint64),
         ("filteredPairs", ctypes.c_uint64), ("msFilter", ctypes.c_double),
         ("msNarrow", ctypes.c_double), ("msWide", ctypes.c_double), ("pairsNarrow", ctypes.c_uint64),
-        ("pairsWide", ctypes.c_uint64), ("cellsWide", ctypes.c_uint64)]
+        ("pairsWide", ctypes.c_uint64), ("cellsWide", ctypes.c_uint64), ("graphLaunches", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -89,10 +89,10 @@ class OicTuning(ctypes.Structure):
     """oic_tuning: DP launch configuration (zeros = defaults)."""
     _fields_ = [("narrowArena", ctypes.c_uint32), ("wideMinLen", ctypes.c_uint32), ("wideThreads", ctypes.c_uint32),
                 ("wideTile", ctypes.c_uint32), ("wideBandW", ctypes.c_uint32), ("wideCtas", ctypes.c_uint32),
-                ("wideArena", ctypes.c_uint64), ("forceWide", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("wideArena", ctypes.c_uint64), ("forceWide", ctypes.c_uint32), ("noGraph", ctypes.c_uint32)]
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 _lib = None

@@ -168,6 +168,13 @@ struct oic_ctx {
 
   oic_tuning tune{};            // DP launch configuration (zeros: defaults)
 
+  // Captured align stage (see align_stage_graph): the executable graph, the events it
+  // records, and the bytes of every parameter baked into it.
+  cudaGraphExec_t      gExec = nullptr;
+  unsigned             gKernels = 0;   // kernel nodes of the graph
+  cudaEvent_t          gEv[3] = {nullptr, nullptr, nullptr};
+  std::vector<uint8_t> gKey;
+
   std::vector<uint32_t> out;   // accumulated records, 6 words each
   oic_stats stats{};
 };
@@ -176,12 +183,14 @@ namespace {
 
 constexpr int kRetrySmaller = 100;   // run_batch: the batch's output did not fit
 
-enum CtrIdx {   // u32 counters
-  cSegCounter = 0, cPairCount, cNodeCount, cSegOvf, cWorkCounter, cAlnOvf, cErr, cRecTotal, cKeep, cNumU32 = 16
+enum CtrIdx {   // u32 counters (cKeep and cKeep + 1: the two bin sizes)
+  cSegCounter = 0, cPairCount, cNodeCount, cSegOvf, cWorkCounter, cAlnOvf, cErr, cRecTotal, cKeep, cKeep2, cWideN,
+  cNumU32 = 16
 };
 constexpr int kSeedStatBase  = 16;   // u64 index: [seeds, segments]
 constexpr int kAlignStatBase = 20;   // u64 index: kStCount entries
 constexpr int kExtStatBase   = 40;
+constexpr int kCellsSnap     = 60;   // u64 index: DP cells after the one-warp bin of a captured batch
 
 uint32_t *ctr32(oic_ctx *c) { return c->dCtr.as<uint32_t>(); }
 unsigned long long *ctr64(oic_ctx *c) { return (unsigned long long *)c->dCtr.as<uint32_t>(); }
@@ -481,7 +490,8 @@ int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t e
     CK(ctx->dFeat.ensure((size_t)nPairs * OIC_FILTER_IN * 2));
     launch_pair_features(ctx->dPairs.as<PairRec>(), nPairs, ctx->dNodes.as<int4>(), ctx->R.len, ctx->T.sread,
                          ctx->dp.kmerLen, ctx->dFeat.p, ctx->st);
-    CK(ctx->dLogit.ensure((size_t)nPairs * sizeof(float)));
+    // Capacity-sized, so the captured align stage's pointer to the scores stays valid.
+    CK(ctx->dLogit.ensure((size_t)std::max(nPairs, ctx->pairCap) * sizeof(float)));
     if (useFilter)
       CK(launch_mlp_forward(ctx->dFilterPrm.p, ctx->dFeat.p, nPairs, ctx->dLogit.as<float>(), nullptr, nullptr,
                             ctx->st));
@@ -552,6 +562,8 @@ int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning
   ao.tierLogit     = tier ? ctx->dLogit.as<float>() : nullptr;
   ao.tierThr       = ctx->filterTierThr;
   ao.tierBudget    = ctx->filterBudget;
+  ao.nWorkDev      = nullptr;
+  ao.workOffDev    = nullptr;
 
   cudaEvent_t ev[4];
   for (auto &x : ev) CK(cudaEventCreate(&x));
@@ -681,6 +693,248 @@ int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning
   return OIC_OK;
 }
 
+template <typename T> void key_add(std::vector<uint8_t> &k, const T &v) {
+  const uint8_t *b = (const uint8_t *)&v;
+  k.insert(k.end(), b, b + sizeof(T));
+}
+
+// The align stage as one captured CUDA graph per context: work keys, the radix sort,
+// the one-warp bin, the overflow hand-over, the CTA bin, the record scan and
+// compaction, all sized for the batch capacity (pairCap) and reading the batch's pair
+// count and bin sizes on the device.  It is captured once and relaunched for every
+// batch; a new capture happens only when a baked-in parameter changes (a buffer was
+// reallocated, the tuning or the filter changed).  The host reads the counters once
+// after the launch; the rare large-arena rerun runs outside the graph.
+int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning &tn, cudaEvent_t evAln0,
+                      cudaEvent_t evAln1, std::vector<uint32_t> &recOut, AlignTimes &at) {
+  int rc = OIC_OK;
+  const bool     useFilter = ctx->filterOn && nPairs > 0;
+  const bool     coll      = ctx->collect != 0;
+  const uint32_t cap       = ctx->pairCap;
+  CK(ctx->dWork.ensure((size_t)cap * 2 * sizeof(uint32_t)));
+  CK(ctx->dCnt.ensure((size_t)cap * sizeof(uint32_t)));
+  CK(ctx->dRecPos.ensure((size_t)cap * sizeof(uint32_t)));
+  CK(ctx->dRec.ensure((size_t)cap * 18 * sizeof(uint32_t)));
+  CK(ctx->dRecOut.ensure((size_t)cap * 18 * sizeof(uint32_t)));
+  CK(ctx->dAlnOvf.ensure((size_t)cap * sizeof(uint32_t)));
+  CK(ctx->dWorkK.ensure((size_t)cap * 8));
+  CK(ctx->dWorkK2.ensure((size_t)cap * 8));
+  CK(ctx->dWorkV2.ensure((size_t)cap * 4));
+  CK(ctx->dWorkScratch.ensure(radix_sort_scratch(cap) + 256));
+  CK(ctx->dScanScratch.ensure(scan_u32_scratch(cap) + 256));
+  if (useFilter) CK(ctx->dLogit.ensure((size_t)cap * sizeof(float)));
+  if (coll) {
+    CK(ctx->dPairCells.ensure((size_t)cap * sizeof(uint32_t)));
+    CK(ctx->dPairExt.ensure((size_t)cap * sizeof(int4)));
+  }
+  AlignConfig an = align_normal(ctx);
+  an.caps.arenaCap = (int)tn.narrowArena;
+  WarpScratch wsN;
+  if ((rc = ensure_align_scratch(ctx, an, false, wsN))) return rc;
+  uint32_t    ctas = 0;
+  AlignCaps   capsG;
+  WarpScratch wsG;
+  if ((rc = ensure_group_scratch(ctx, tn, false, ctas, capsG, wsG))) return rc;
+  for (cudaEvent_t &e : ctx->gEv)
+    if (!e) CK(cudaEventCreate(&e));
+
+  AlignOut ao{};
+  ao.rec           = ctx->dRec.as<uint32_t>();
+  ao.cnt           = ctx->dCnt.as<uint32_t>();
+  ao.overflow      = ctx->dAlnOvf.as<uint32_t>();
+  ao.overflowCount = ctr32(ctx) + cAlnOvf;
+  ao.stats         = ctr64(ctx) + kAlignStatBase;
+  ao.err           = ctr32(ctx) + cErr;
+  ao.cells         = coll ? ctx->dPairCells.as<uint32_t>() : nullptr;
+  ao.ext           = coll ? ctx->dPairExt.as<int4>() : nullptr;
+  const bool tier  = useFilter && ctx->filterTierThr > ctx->filterLogitThr;
+  ao.tierLogit     = tier ? ctx->dLogit.as<float>() : nullptr;
+  ao.tierThr       = ctx->filterTierThr;
+  ao.tierBudget    = ctx->filterBudget;
+  AlignOut aoN = ao, aoW = ao;
+  aoN.nWorkDev   = ctr32(ctx) + cKeep;    // one-warp bin: work[0 .. bin 0)
+  aoW.nWorkDev   = ctr32(ctx) + cWideN;   // CTA bin: work[bin 0 .. bin 0 + wideN)
+  aoW.workOffDev = ctr32(ctx) + cKeep;
+  const float *logit = useFilter ? ctx->dLogit.as<float>() : nullptr;
+  const int    threads = (int)tn.wideThreads;
+
+  std::vector<uint8_t> key;
+  key_add(key, aoN);
+  key_add(key, aoW);
+  key_add(key, logit);
+  key_add(key, ctx->filterLogitThr);
+  key_add(key, tn);
+  key_add(key, cap);
+  key_add(key, ctas);
+  key_add(key, capsG);
+  key_add(key, wsN);
+  key_add(key, wsG);
+  key_add(key, an);
+  key_add(key, ctx->R);
+  key_add(key, ctx->T);
+  key_add(key, ctx->dp);
+  const void *bufs[] = {ctx->dPairs.p, ctx->dNodes.p, ctx->dWork.p, ctx->dRecPos.p, ctx->dRecOut.p, ctx->dWorkK.p,
+                        ctx->dWorkK2.p, ctx->dWorkV2.p, ctx->dWorkScratch.p, ctx->dScanScratch.p, ctx->dEml.p,
+                        ctx->dCtr.p};
+  key_add(key, bufs);
+
+  if (!ctx->gExec || key != ctx->gKey) {
+    if (ctx->gExec) {
+      cudaGraphExecDestroy(ctx->gExec);
+      ctx->gExec = nullptr;
+    }
+    const unsigned long long launches0 = g_launches;   // capture launches nothing
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t s = ctx->st;
+    cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, 4 * sizeof(uint32_t), s);   // work, aln ovf, err, rec total
+    cudaMemsetAsync(ctr32(ctx) + cKeep, 0, 3 * sizeof(uint32_t), s);          // bins, CTA-bin length
+    cudaMemsetAsync(ctr64(ctx) + kAlignStatBase, 0, kStCount * sizeof(unsigned long long), s);
+    launch_work_keys(ctx->dPairs.as<PairRec>(), cap, logit, ctx->filterLogitThr, ctx->R.len, ctx->T.sread,
+                     tn.wideMinLen, ctr32(ctx) + cKeep, ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), s,
+                     ctr32(ctx) + cPairCount);
+    radix_sort_u64_u32(ctx->dWorkK.as<u64>(), ctx->dWork.as<uint32_t>(), ctx->dWorkK2.as<u64>(),
+                       ctx->dWorkV2.as<uint32_t>(), cap, 32, ctx->dWorkScratch.p, s, ctr32(ctx) + cPairCount);
+    cudaMemsetAsync(ctx->dCnt.p, 0, (size_t)cap * sizeof(uint32_t), s);
+    if (coll) {
+      cudaMemsetAsync(ctx->dPairCells.p, 0, (size_t)cap * sizeof(uint32_t), s);
+      cudaMemsetAsync(ctx->dPairExt.p, 0, (size_t)cap * sizeof(int4), s);
+    }
+    cudaEventRecordWithFlags(ctx->gEv[0], s, cudaEventRecordExternal);   // recorded at every replay
+    launch_align(an.bandW, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
+                 ctx->dWork.as<uint32_t>(), 0, ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), wsN, an.caps,
+                 an.warps, aoN, s);
+    cudaMemcpyAsync(ctr64(ctx) + kCellsSnap, ctr64(ctx) + kAlignStatBase + kStCells, sizeof(unsigned long long),
+                    cudaMemcpyDeviceToDevice, s);
+    cudaEventRecordWithFlags(ctx->gEv[1], s, cudaEventRecordExternal);   // recorded at every replay
+    launch_append_overflow(ctx->dWork.as<uint32_t>(), ctr32(ctx) + cKeep, ctx->dAlnOvf.as<uint32_t>(),
+                           ctr32(ctx) + cAlnOvf, ctr32(ctx) + cWideN, ctr32(ctx) + cWorkCounter, ctr32(ctx) + cErr,
+                           s);
+    launch_align_group(threads, (int)tn.wideTile, capsG.bandW, (int)ctas, ctx->R, ctx->T, ctx->dp,
+                       ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(), ctx->dWork.as<uint32_t>(), 0,
+                       ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), wsG, capsG, aoW, s);
+    cudaEventRecordWithFlags(ctx->gEv[2], s, cudaEventRecordExternal);   // recorded at every replay
+    scan_u32(ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), cap, ctr32(ctx) + cRecTotal,
+             ctx->dScanScratch.p, s);
+    launch_compact_records(ctx->dRec.as<uint32_t>(), ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), cap,
+                           ctx->dRecOut.as<uint32_t>(), s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+    g_launches    = launches0;
+    ctx->gKernels = 0;
+    if (e == cudaSuccess) {
+      size_t nn = 0;
+      cudaGraphGetNodes(g, nullptr, &nn);
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+      for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ctx->gKernels++;
+      }
+      e = cudaGraphInstantiate(&ctx->gExec, g, 0);
+    }
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ctx->gExec = nullptr;
+      return fail(ctx, OIC_ERR_CUDA, "align graph capture: %s", cudaGetErrorString(e));
+    }
+    ctx->gKey = key;
+  }
+
+  CK(cudaEventRecord(evAln0, ctx->st));
+  CK(cudaGraphLaunch(ctx->gExec, ctx->st));
+  g_launches += ctx->gKernels;
+  uint32_t           h[16];
+  unsigned long long snap = 0;
+  CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&snap, ctr64(ctx) + kCellsSnap, sizeof(snap), cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "align graph"))) return rc;
+  const uint32_t nNarrow = h[cKeep], nWide = h[cKeep2], nW = h[cWideN];
+  at.pairsNarrow += nNarrow;
+  at.pairsWide += nW;
+  float a0 = 0, a1 = 0;
+  if (cudaEventElapsedTime(&a0, ctx->gEv[0], ctx->gEv[1]) != cudaSuccess ||
+      cudaEventElapsedTime(&a1, ctx->gEv[1], ctx->gEv[2]) != cudaSuccess) {
+    a0 = a1 = 0;
+    cudaGetLastError();
+  }
+  at.msNarrow += a0;
+  at.msWide += a1;
+  uint32_t nRec = h[cRecTotal];
+  if (h[cAlnOvf]) {
+    // CTA-bin pairs over the CTA arena: the large-arena rerun, then the records again.
+    const uint32_t o = h[cAlnOvf];
+    if (verbose()) fprintf(stderr, "oic: %u pairs rerun with the large DP arena\n", o);
+    CK(cudaMemcpyAsync(ctx->dWork.as<uint32_t>(), ctx->dAlnOvf.p, o * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                       ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cAlnOvf, 0, sizeof(uint32_t), ctx->st));
+    CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, sizeof(uint32_t), ctx->st));
+    uint32_t    ctasH = 0;
+    AlignCaps   capsH;
+    WarpScratch wsH;
+    if ((rc = ensure_group_scratch(ctx, tn, true, ctasH, capsH, wsH))) return rc;
+    cudaEvent_t h0, h1;
+    cudaEventCreate(&h0);
+    cudaEventCreate(&h1);
+    cudaEventRecord(h0, ctx->st);
+    launch_align_group((int)std::max<uint32_t>(tn.wideThreads, 512), (int)tn.wideTile, capsH.bandW,
+                       (int)std::min<uint32_t>(ctasH, o), ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(),
+                       ctx->dPairs.as<PairRec>(), ctx->dWork.as<uint32_t>(), o, ctr32(ctx) + cWorkCounter,
+                       ctx->dNodes.as<int4>(), wsH, capsH, ao, ctx->st);
+    cudaEventRecord(h1, ctx->st);
+    CK(scan_u32(ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), cap, ctr32(ctx) + cRecTotal,
+                ctx->dScanScratch.p, ctx->st));
+    launch_compact_records(ctx->dRec.as<uint32_t>(), ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), cap,
+                           ctx->dRecOut.as<uint32_t>(), ctx->st);
+    CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
+    rc = sync_check(ctx, "align kernel (large arena)");
+    float hm = 0;
+    cudaEventElapsedTime(&hm, h0, h1);
+    cudaEventDestroy(h0);
+    cudaEventDestroy(h1);
+    if (rc) return rc;
+    at.msWide += hm;
+    at.pairsWide += o;
+    if (h[cAlnOvf])
+      return fail(ctx, OIC_ERR_OVERFLOW,
+                  "a read pair needs a wider DP band or deeper traceback than the engine holds (err 0x%x)", h[cErr]);
+    nRec = h[cRecTotal];
+  }
+  CK(cudaEventRecord(evAln1, ctx->st));
+  if (nRec) {
+    size_t old = recOut.size();
+    recOut.resize(old + (size_t)nRec * 6);
+    CK(cudaMemcpyAsync(recOut.data() + old, ctx->dRecOut.p, (size_t)nRec * 6 * sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  }
+  unsigned long long st64[2 + kStCount];
+  CK(cudaMemcpyAsync(st64, ctr64(ctx) + kSeedStatBase, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(st64 + 2, ctr64(ctx) + kAlignStatBase, kStCount * sizeof(unsigned long long),
+                     cudaMemcpyDeviceToHost, ctx->st));
+  if ((rc = sync_check(ctx, "record download"))) return rc;
+  at.cellsWide += st64[2 + kStCells] - snap;
+
+  oic_stats &S = ctx->stats;
+  S.seeds += st64[0];
+  S.candidatePairs += nPairs;
+  S.nodes += nNodes;
+  S.kmerHitsWithoutOlap += st64[2 + kStWithoutOlap];
+  S.kmerHitsWithOlap += st64[2 + kStWithOlap];
+  S.kmerHitsSkipped += st64[2 + kStSkipped];
+  S.multiOverlap += st64[2 + kStMulti];
+  S.totalOverlaps += st64[2 + kStTotal];
+  S.containedOverlaps += st64[2 + kStContained];
+  S.dovetailOverlaps += st64[2 + kStDovetail];
+  S.dpCells += st64[2 + kStCells];
+  S.slideBases += st64[2 + kStSlides];
+  S.extensions += st64[2 + kStExtensions];
+  S.dpRows += st64[2 + kStRows];
+  S.dpCellsNoOverlap += st64[2 + kStCellsNoOlap];
+  if (useFilter) S.filteredPairs += nPairs - nNarrow - nWide;
+  S.graphLaunches++;
+  return OIC_OK;
+}
+
 // Process one batch of eligible ref reads against the loaded block.  Returns OIC_OK,
 // or kRetrySmaller when the batch's output did not fit (caller splits the batch).
 int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
@@ -691,7 +945,9 @@ int run_batch(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t ev
   const bool useFilter = ctx->filterOn && nPairs > 0;
   const oic_tuning tn = resolved_tuning(ctx);
   AlignTimes at;
-  if ((rc = align_stage(ctx, nPairs, nNodes, tn, evSeed1, evAln1, ctx->out, at))) return rc;
+  rc = tn.noGraph || nPairs == 0 ? align_stage(ctx, nPairs, nNodes, tn, evSeed1, evAln1, ctx->out, at)
+                                 : align_stage_graph(ctx, nPairs, nNodes, tn, evSeed1, evAln1, ctx->out, at);
+  if (rc) return rc;
   float a = 0, b = 0;
   cudaEventElapsedTime(&a, evSeed0, evSeed1);
   cudaEventElapsedTime(&b, evSeed1, evAln1);
@@ -879,6 +1135,9 @@ void oic_destroy(oic_ctx *ctx) {
                     &ctx->dRowsG,    &ctx->dRowsG2,     &ctx->dFilterPrm,  &ctx->dFeat,      &ctx->dLogit,
                     &ctx->dPairCells, &ctx->dPairExt};
   for (DevBuf *b : bufs) b->release();
+  if (ctx->gExec) cudaGraphExecDestroy(ctx->gExec);
+  for (cudaEvent_t e : ctx->gEv)
+    if (e) cudaEventDestroy(e);
   if (ctx->evF0) cudaEventDestroy(ctx->evF0);
   if (ctx->evF1) cudaEventDestroy(ctx->evF1);
   if (ctx->st) cudaStreamDestroy(ctx->st);

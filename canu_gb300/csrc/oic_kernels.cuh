@@ -100,6 +100,8 @@ struct AlignOut {
   const float *tierLogit;   // optional: pairs scored below tierThr stop once tierBudget
   float        tierThr;     // extensions have run without finding an overlap
   int          tierBudget;
+  const u32   *nWorkDev;    // optional: the work list's length, read on the device
+  const u32   *workOffDev;  // optional: the work list starts at work + *workOffDev
 };
 
 enum StatIdx {
@@ -138,7 +140,11 @@ void launch_extend_batch(int bandW, ReadsDev R, DevParams P, const int *eml, con
 // the caller) get the sizes of bins 0 and 1.
 void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
                       const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys, u32 *vals,
-                      cudaStream_t st);
+                      cudaStream_t st, const u32 *nDev = nullptr);
+// Append the one-warp overflow behind the CTA bin's own pairs on the device (see
+// append_overflow_kernel in oic_pairs.cu).
+void launch_append_overflow(u32 *work, const u32 *binCount, const u32 *ovf, u32 *ovfCount, u32 *wideN,
+                            u32 *workCounter, u32 *err, cudaStream_t st);
 
 // ---------------- learned candidate filter (oic_filter.cu) ----------------
 // feat: n x 80 FP16 rows (67 features, 13 zeros) of the candidate pairs.

@@ -425,6 +425,9 @@ static __device__ __forceinline__ void align_loop(WarpDP &w, PairSmem &ps, const
                                                   const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter,
                                                   const int4 *nodes, const AlignOut &out) {
   const int lane = threadIdx.x & 31;
+  // Inside a captured graph the list's length and start are known only on the device.
+  if (out.nWorkDev) nWork = *out.nWorkDev;
+  if (out.workOffDev) work += *out.workOffDev;
   if (lane == 0)
     for (int i = 0; i < kStCount; i++) ps.acc.v[i] = 0;
   __syncwarp();
@@ -527,7 +530,8 @@ __global__ void __launch_bounds__(512, 1) align_group_kernel(ReadsDev R, TableDe
 // of bins 0 and 1.
 __global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
                                  const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys,
-                                 u32 *vals) {
+                                 u32 *vals, const u32 *nDev) {
+  if (nDev && *nDev < n) n = *nDev;
   const u32 stride = gridDim.x * blockDim.x;
   const int lane   = threadIdx.x & 31;
   for (u32 i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -549,6 +553,25 @@ __global__ void work_keys_kernel(const PairRec *pairs, u32 n, const float *logit
       if (b0) atomicAdd(&binCount[0], (u32)__popc(b0));
       if (b1) atomicAdd(&binCount[1], (u32)__popc(b1));
     }
+  }
+}
+
+// The CTA-bin list of a captured batch: the one-warp overflow (ovf[0 .. *ovfCount))
+// appended behind the bin's own pairs (work[b0 .. b0 + b1), b0/b1 = binCount[0..1]);
+// its length goes to *wideN, and the counters the CTA pass uses are cleared.  One block.
+__global__ void append_overflow_kernel(u32 *work, const u32 *binCount, const u32 *ovf, u32 *ovfCount, u32 *wideN,
+                                       u32 *workCounter, u32 *err) {
+  __shared__ u32 n;
+  if (threadIdx.x == 0) n = *ovfCount;
+  __syncthreads();
+  const u32 b0 = binCount[0], b1 = binCount[1];
+  for (u32 i = threadIdx.x; i < n; i += blockDim.x) work[b0 + b1 + i] = ovf[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *wideN       = b1 + n;
+    *ovfCount    = 0;
+    *workCounter = 0;
+    *err         = 0;
   }
 }
 
@@ -579,7 +602,7 @@ size_t align_smem_bytes(int) { return (size_t)kAlignWarpsSmall * 2 * 512 * sizeo
 void launch_align(int, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs, const u32 *work,
                   u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap, int nWarps,
                   AlignOut out, cudaStream_t st) {
-  if (nWork == 0) return;
+  if (nWork == 0 && !out.nWorkDev) return;
   const int    blocks = (nWarps + kAlignWarpsSmall - 1) / kAlignWarpsSmall;
   const size_t smem   = align_smem_bytes(512);
   cap.bandW           = 512;
@@ -592,7 +615,7 @@ void launch_align(int, ReadsDev R, TableDev T, DevParams P, const int *eml, cons
 void launch_align_group(int threads, int U, int bandW, int ctas, ReadsDev R, TableDev T, DevParams P, const int *eml,
                         const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes,
                         WarpScratch sc, AlignCaps cap, AlignOut out, cudaStream_t st) {
-  if (nWork == 0) return;
+  if (nWork == 0 && !out.nWorkDev) return;
   cap.bandW         = bandW;
   const size_t smem = (size_t)2 * bandW * sizeof(int);
   cudaFuncSetAttribute(align_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -628,11 +651,18 @@ void launch_extend_group(int threads, int U, int bandW, int ctas, ReadsDev R, De
 
 void launch_work_keys(const PairRec *pairs, u32 n, const float *logit, float logitThr, const u32 *readLen,
                       const u32 *strRead, u32 wideMinLen, u32 *binCount, unsigned long long *keys, u32 *vals,
-                      cudaStream_t st) {
+                      cudaStream_t st, const u32 *nDev) {
   if (n == 0) return;
   unsigned g = (n + 255) / 256;
   if (g > 65535u * 8) g = 65535u * 8;
-  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, readLen, strRead, wideMinLen, binCount, keys, vals);
+  work_keys_kernel<<<g, 256, 0, st>>>(pairs, n, logit, logitThr, readLen, strRead, wideMinLen, binCount, keys, vals,
+                                      nDev);
+  g_launches++;
+}
+
+void launch_append_overflow(u32 *work, const u32 *binCount, const u32 *ovf, u32 *ovfCount, u32 *wideN,
+                            u32 *workCounter, u32 *err, cudaStream_t st) {
+  append_overflow_kernel<<<1, 1024, 0, st>>>(work, binCount, ovf, ovfCount, wideN, workCounter, err);
   g_launches++;
 }
 

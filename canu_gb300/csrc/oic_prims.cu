@@ -128,8 +128,10 @@ constexpr int kSortTile    = kSortThreads * kSortItems;   // 4096
 constexpr int kDigits      = 256;
 
 __global__ void __launch_bounds__(kSortThreads) radix_upsweep_kernel(const unsigned long long *keys, uint64_t n, int shift,
-                                                                     uint32_t *hist, uint32_t nTiles) {
+                                                                     uint32_t *hist, uint32_t nTiles,
+                                                                     const uint32_t *nDev) {
   __shared__ uint32_t h[kSortWarps][kDigits];
+  if (nDev && *nDev < n) n = *nDev;
   const int wid = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * kDigits; i += kSortThreads) (&h[0][0])[i] = 0;
   __syncthreads();
@@ -151,8 +153,9 @@ __global__ void __launch_bounds__(kSortThreads) radix_upsweep_kernel(const unsig
 __global__ void __launch_bounds__(kSortThreads) radix_downsweep_kernel(const unsigned long long *keysIn, const uint32_t *valsIn,
                                                                        unsigned long long *keysOut, uint32_t *valsOut, uint64_t n,
                                                                        int shift, const uint32_t *offsets,
-                                                                       uint32_t nTiles) {
+                                                                       uint32_t nTiles, const uint32_t *nDev) {
   __shared__ uint32_t cnt[kSortWarps][kDigits];
+  if (nDev && *nDev < n) n = *nDev;
   __shared__ uint32_t tileBase[kDigits];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * kDigits; i += kSortThreads) (&cnt[0][0])[i] = 0;
@@ -215,7 +218,7 @@ size_t radix_sort_scratch(uint64_t n) {
 }
 
 cudaError_t radix_sort_u64_u32(unsigned long long *keys, uint32_t *vals, unsigned long long *keysAlt, uint32_t *valsAlt, uint64_t n,
-                               int bits, void *scratch, cudaStream_t st) {
+                               int bits, void *scratch, cudaStream_t st, const uint32_t *nDev) {
   if (n <= 1 || bits <= 0) return cudaSuccess;
   uint64_t  nTiles = (n + kSortTile - 1) / kSortTile;
   uint64_t  nh     = nTiles * kDigits;
@@ -225,12 +228,12 @@ cudaError_t radix_sort_u64_u32(unsigned long long *keys, uint32_t *vals, unsigne
   uint32_t *vs = vals, *vd = valsAlt;
   int       passes = 0;
   for (int shift = 0; shift < bits; shift += 8, passes++) {
-    radix_upsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, n, shift, hist, (uint32_t)nTiles);
+    radix_upsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, n, shift, hist, (uint32_t)nTiles, nDev);
     g_launches++;
     cudaError_t e = scan_u32(hist, hist, nh, nullptr, scanSc, st);
     if (e != cudaSuccess) return e;
     radix_downsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, vs, kd, vd, n, shift, hist,
-                                                                       (uint32_t)nTiles);
+                                                                       (uint32_t)nTiles, nDev);
     g_launches++;
     unsigned long long *tk = ks; ks = kd; kd = tk;
     uint32_t *tv = vs; vs = vd; vd = tv;

@@ -20,8 +20,10 @@ cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint64_t n, uint32_t *to
 // Scratch bytes radix_sort needs for n elements (double buffers are separate).
 size_t radix_sort_scratch(uint64_t n);
 // Stable ascending sort of keys/vals on key bits [0, bits).  keys/vals are sorted in
-// place; keysAlt/valsAlt are buffers of the same size used for ping-pong.
+// place; keysAlt/valsAlt are buffers of the same size used for ping-pong.  With nDev
+// non-null the launches are sized for n keys and sort the first min(n, *nDev) (a count
+// known only on the device, e.g. inside a captured graph).
 cudaError_t radix_sort_u64_u32(unsigned long long *keys, uint32_t *vals, unsigned long long *keysAlt, uint32_t *valsAlt, uint64_t n,
-                               int bits, void *scratch, cudaStream_t st);
+                               int bits, void *scratch, cudaStream_t st, const uint32_t *nDev = nullptr);
 
 }  // namespace oic

@@ -13,7 +13,7 @@
 //     blocks as ovFile does (default: the six-word records unframed);
 //   * --gpu-tune key=value[,key=value...] sets DP launch fields of oic_tuning
 //     (narrowArena, wideMinLen, wideThreads, wideTile, wideBandW, wideCtas, wideArena,
-//     forceWide), and --gpu-autotune <n> times the DP grid on the first n ref reads
+//     forceWide, noGraph), and --gpu-autotune <n> times the DP grid on the first n ref reads
 //     against the first hash block and keeps the fastest configuration (oic_autotune).
 //     Neither changes the records.
 #include <cerrno>
@@ -155,6 +155,7 @@ bool parseTuning(const char *s, oic_tuning &t) {
     else if (k == "wideCtas") t.wideCtas = (uint32_t)v;
     else if (k == "wideArena") t.wideArena = v;
     else if (k == "forceWide") t.forceWide = (uint32_t)v;
+    else if (k == "noGraph") t.noGraph = (uint32_t)v;
     else return false;
     if (q == std::string::npos) break;
     p = q + 1;

@@ -73,6 +73,7 @@ typedef struct oic_stats {
   double   msNarrow, msWide;                       /* device time of the one-warp and CTA DP bins */
   uint64_t pairsNarrow, pairsWide;                 /* pairs run in each bin (reruns in the CTA bin) */
   uint64_t cellsWide;                              /* DP cells of the CTA bin */
+  uint64_t graphLaunches;                          /* batches whose DP stage ran as one captured CUDA graph */
 } oic_stats;
 
 typedef struct oic_ctx oic_ctx;
@@ -257,7 +258,8 @@ typedef struct oic_tuning {
   uint32_t wideCtas;      /* CTAs of the CTA bin (default: 2 per SM) */
   uint64_t wideArena;     /* kept DP cells per CTA of the CTA bin (default: 2^24, less if memory is short) */
   uint32_t forceWide;     /* testing: every pair goes to the CTA bin (0 / 1) */
-  uint32_t reserved;
+  uint32_t noGraph;       /* 1: launch the DP stage kernel by kernel with host-read sizes instead of
+                             relaunching its captured CUDA graph (same records) */
 } oic_tuning;
 
 int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t);   /* NULL: defaults */

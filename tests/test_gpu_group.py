@@ -94,3 +94,32 @@ def test_autotune_reports_the_grid_and_keeps_records(built, golden_inputs):
     best = min(lines, key=lambda l: l["msTotal"])
     assert tun["wideThreads"] == best["wideThreads"] and tun["wideTile"] == best["wideTile"]
     assert np.array_equal(recs, base)
+
+
+def test_captured_graph_matches_kernel_by_kernel(built, tmp_path_factory):
+    """The DP stage relaunched as one captured CUDA graph gives the records and counters
+    of the kernel-by-kernel launch, with and without the learned filter."""
+    import os
+    from canu_gb300 import filter_train, workloads
+    d = str(tmp_path_factory.mktemp("graph"))
+    db, skip = workloads.generate("c2", d, scale=0.02, seed=7)
+    fpath = os.path.join(os.path.dirname(oic.__file__), "filter_c2.npz")
+    params, thr, full, meta = filter_train.load(fpath)
+
+    def run(no_graph, filt):
+        with oic.Overlapper(workloads.params("c2")) as ov:
+            ov.set_reads_seqdb(db)
+            ov.set_skip_kmers(workloads.read_skip(skip))
+            ov.set_tuning(noGraph=no_graph, wideArena=SMALL_ARENA, wideCtas=64)
+            if filt:
+                ov.set_filter(params, thr, full, meta["budget"])
+            ov.run()
+            return oic.sort_records(ov.overlaps()), ov.stats()
+
+    for filt in (False, True):
+        a, sa = run(0, filt)
+        b, sb = run(1, filt)
+        assert len(a) > 1000 and np.array_equal(a, b)
+        for k in ("dpCells", "extensions", "kmerHitsWithOlap", "kmerHitsWithoutOlap", "filteredPairs", "slideBases"):
+            assert sa[k] == sb[k], k
+        assert sa["graphLaunches"] > 0 and sb["graphLaunches"] == 0
