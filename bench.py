@@ -383,6 +383,10 @@ def main():
     mean_len = float(ln.mean())
     alg_bytes = pairs * (32 + 72 + 4 + 2 * mean_len / 4) + nodes * 16
     achieved = alg_bytes / (ms_align / 1000.0) / 1e9
+    # DRAM bytes per DP cell of the one-warp DP kernel, from one ncu capture of a 1/50
+    # scale c2 launch (6.39 GB read + 18.58 GB written for 6.598 G cells; the figures and
+    # the command are in profiles/align_kernel_c2_scale0.02_ncu.md), scaled to this job.
+    traffic = 3.784 * cells
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
     int_ops = 6 * cells + slides / 16.0
@@ -402,7 +406,9 @@ def main():
                 "d2h_bytes_per_step": int(n_ov * 24), "pinned": pinned_ok, "timing": "wall clock"},
         "roofline": {"bound": "hbm", "kernel": "align_kernel", "achieved": achieved,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-                     "traffic": None, "peak_kind": peak_kind,
+                     "traffic": traffic, "traffic_basis": "ncu dram read+write per DP cell of a 1/50-scale c2 "
+                                                          "launch x this job's DP cells (bytes per job)",
+                     "peak_kind": peak_kind,
                      "int_ops": {"achieved_tops": int_ops / (ms_align / 1000.0) / 1e12, "peak_tops": int_peak,
                                  "frac": int_ops / (ms_align / 1000.0) / 1e12 / int_peak,
                                  "basis": "6 INT ops per DP cell + 1/16 per slide base; peak = 152 SMs x 128 "
