@@ -121,15 +121,21 @@ def dist():
     return ws, rank, local
 
 
-def barrier_max(value, ws):
-    """max over ranks (and a barrier)."""
+def barrier_max(value, ws, device="cuda"):
+    """max over ranks (and a barrier); device "cpu" for a gloo process group."""
     if ws == 1:
         return value
     import torch
     import torch.distributed as td
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     td.all_reduce(t, op=td.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(units_per_rank, seconds, ws, device="cuda"):
+    """Whole-job rate of independent replicas: every rank's units over the slowest
+    rank's time (the ranks run the same workload, so units_per_rank is this rank's)."""
+    return ws * units_per_rank / barrier_max(seconds, ws, device)
 
 
 # ----------------------------------------------------------------------------------
@@ -373,9 +379,8 @@ def main():
     st0 = res[0][0]
     n_ov = st0["totalOverlaps"]
     ms_dev_max = barrier_max(ms_dev, ws)
-    s_e2e_max = barrier_max(s_e2e, ws)
-    value = ws * n_ov / (ms_dev_max / 1000.0)
-    e2e = ws * n_ov / s_e2e_max
+    value = replica_rate(n_ov, ms_dev / 1000.0, ws)
+    e2e = replica_rate(n_ov, s_e2e, ws)
 
     # Roofline of the dominant kernel, the pair DP (align_kernel).
     ms_align = statistics.mean(r[0]["msAlign"] for r in res)

@@ -1,0 +1,40 @@
+"""The drop-in command line's argument handling (no GPU needed: every case ends before
+a context is created)."""
+import subprocess
+
+import pytest
+
+
+def run(built, *args):
+    return subprocess.run([built["cli"]] + list(args), stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+
+
+def test_unknown_flag_prints_usage_and_fails(built, tmp_path):
+    # As in overlapInCore.C:387-393, the first unrecognised argument is the store path
+    # and any later one is an unknown option.
+    r = run(built, "-k", "22", "-o", str(tmp_path / "o.ovb"), "store", "--bogus")
+    assert r.returncode == 1 and "Unknown option '--bogus'" in r.stderr and "USAGE" in r.stderr
+
+
+def test_missing_kmer_size_and_output_are_errors(built):
+    r = run(built, "store")
+    assert r.returncode == 1
+    assert "No kmer length supplied" in r.stderr and "No output file name specified" in r.stderr
+
+
+def test_overlap_cap_is_rejected(built, tmp_path):
+    # -l n makes read pairs depend on each other's processing order (a documented
+    # difference); -l 0 (no cap) is accepted.
+    r = run(built, "-k", "22", "-l", "5", "-o", str(tmp_path / "o.ovb"), "store")
+    assert r.returncode == 1 and "-l (per-read overlap limit) is not supported" in r.stderr
+
+
+@pytest.mark.parametrize("tune", ["wideThreads", "nope=3", "wideTile=2,bad=1"])
+def test_bad_gpu_tune_is_rejected(built, tmp_path, tune):
+    r = run(built, "-k", "22", "--gpu-tune", tune, "-o", str(tmp_path / "o.ovb"), "store")
+    assert r.returncode == 1 and "bad --gpu-tune value" in r.stderr
+
+
+def test_missing_store_is_reported(built, tmp_path):
+    r = run(built, "-k", "22", "-o", str(tmp_path / "o.ovb"), str(tmp_path / "no_such.seqdb"))
+    assert r.returncode == 1 and "Failed to load read container" in r.stderr
