@@ -321,16 +321,18 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0
     if (L2 == INT_MAX) break;
     const int R2 = __reduce_max_sync(0xffffffffu, myR);
 
-    // Largest value on the kept band (forward.C:284-289); the Max_Score test that uses
-    // it runs once after the rows (max_score_rows).
-    int myV = -1;
-    for (int d = L2 + lane; d <= R2; d += 32) myV = max(myV, cv[d]);
-    const int rowMax = __reduce_max_sync(0xffffffffu, myV);
-
-    // Keep the band for the traceback.
+    // Keep the band for the traceback, and take its largest value on the way
+    // (forward.C:284-289); the Max_Score test that uses it runs once after the rows
+    // (max_score_rows).
     const int cnt = R2 - L2 + 1;
     if (used + cnt > w.cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
-    for (int d = L2 + lane; d <= R2; d += 32) w.sc.arena[used + d - L2] = cv[d];
+    int myV = -1;
+    for (int d = L2 + lane; d <= R2; d += 32) {
+      const int v = cv[d];
+      myV         = max(myV, v);
+      w.sc.arena[used + d - L2] = v;
+    }
+    const int rowMax = __reduce_max_sync(0xffffffffu, myV);
     if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
     used += cnt;
     int *t = prev;
@@ -439,13 +441,15 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
     o.cells += (unsigned long long)width;
     if (L2 == INT_MAX) break;
 
+    // Keep the band for the traceback and take its largest value on the way.
+    const int cnt = R2 - L2 + 1;
+    if (used + cnt > cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
     int myV = -1;
-    for (int d0 = Lc + tid * U; d0 <= Rc; d0 += nThr * U)
-#pragma unroll
-      for (int k = 0; k < U; k++) {
-        const int d = d0 + k;
-        if (d >= L2 && d <= R2) myV = max(myV, cv[d]);
-      }
+    for (int d = L2 + tid; d <= R2; d += nThr) {
+      const int v = cv[d];
+      myV         = max(myV, v);
+      sc.arena[used + d - L2] = v;
+    }
     {
       const int wV = __reduce_max_sync(0xffffffffu, myV);
       if (lane == 0) red[wid][3] = wV;
@@ -453,10 +457,6 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
     group_bar(2, nThr);
     int rowMax = -1;
     for (int i = 0; i < nW; i++) rowMax = max(rowMax, red[i][3]);
-
-    const int cnt = R2 - L2 + 1;
-    if (used + cnt > cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
-    for (int d = L2 + tid; d <= R2; d += nThr) sc.arena[used + d - L2] = cv[d];
     if (tid == 0) sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
     used += cnt;
     int *t = prev;

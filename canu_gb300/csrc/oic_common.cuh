@@ -72,14 +72,15 @@ __device__ __forceinline__ SeqView make_view(const ReadsDev &R, u32 readIdx, int
   return v;
 }
 
-// 32 bases starting at global base index g (base g in bits 0-1).
+// 32 bases starting at global base index g (base g in bits 0-1).  Both words are
+// always read (the arrays end with two spare words), and the high word's shift is
+// split in two so that sh = 0 needs no branch: (hi << 1) << 63 is 0.
 __device__ __forceinline__ u64 load_win(const u64 *w, i64 g) {
-  i64 wi = g >> 5;
-  int sh = (int)(g & 31) * 2;
-  u64 lo = __ldg(w + wi);
-  if (sh == 0) return lo;
-  u64 hi = __ldg(w + wi + 1);
-  return (lo >> sh) | (hi << (64 - sh));
+  const i64 wi = g >> 5;
+  const int sh = (int)(g & 31) * 2;
+  const u64 lo = __ldg(w + wi);
+  const u64 hi = __ldg(w + wi + 1);
+  return (lo >> sh) | ((hi << 1) << (63 - sh));
 }
 
 // 32 bases g, g-1, ..., g-31 (base g in bits 0-1; the two bits of each base come out
