@@ -30,7 +30,7 @@ EXPORTS = (
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
     "oic_extend_batch_noalloc", "oic_set_filter", "oic_collect_pairs", "oic_num_pairs", "oic_get_pairs",
     "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam", "oic_set_tuning", "oic_get_tuning",
-    "oic_autotune",
+    "oic_autotune", "oic_count_kmers",
 )
 
 # Learned candidate filter (include/oic_gpu.h): feature row width, hidden width and the
@@ -134,6 +134,7 @@ def library():
         lib.oic_set_tuning.argtypes = [vp, P(OicTuning)]
         lib.oic_get_tuning.argtypes = [vp, P(OicTuning)]
         lib.oic_autotune.argtypes = [vp, U32, U32, vp, U32, P(U32)]
+        lib.oic_count_kmers.argtypes = [vp, U32, U32, U32, vp, vp, U64, P(U64)]
         lib.oic_last_error.argtypes = [vp]
         lib.oic_last_error.restype = ctypes.c_char_p
         _lib = lib
@@ -312,6 +313,22 @@ class Overlapper:
         t = OicTuning()
         self._check(self._lib.oic_get_tuning(self._ctx, ctypes.byref(t)))
         return t.as_dict()
+
+    def count_kmers(self, bgn, end, min_count):
+        """Canonical k-mers of reads [bgn, end] seen at least min_count times:
+        (list of k-mer strings, uint32 counts), ascending canonical 2-bit key."""
+        n = ctypes.c_uint64()
+        rc = self._lib.oic_count_kmers(self._ctx, bgn, end, min_count, None, None, 0, ctypes.byref(n))
+        if rc not in (OIC_OK, OIC_ERR_OVERFLOW):
+            self._check(rc)
+        k = self.params.kmerLen
+        buf = np.zeros(n.value * k, dtype=np.uint8)
+        cnt = np.zeros(n.value, dtype=np.uint32)
+        if n.value:
+            self._check(self._lib.oic_count_kmers(self._ctx, bgn, end, min_count, _ptr(buf), _ptr(cnt), n.value,
+                                                  ctypes.byref(n)))
+        s = buf.tobytes().decode()
+        return [s[i * k:(i + 1) * k] for i in range(n.value)], cnt
 
     def autotune(self, bgn, end, max_lines=64):
         """Time the DP grid on ref reads [bgn, end] of the loaded block; sets the fastest.

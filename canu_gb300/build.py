@@ -7,6 +7,7 @@ Outputs (git-ignored) go to canu_gb300/_build/:
     liboic_gpu.so      the C-ABI library (include/oic_gpu.h), sm_103a kernels
     overlapInCore      the drop-in command line, linked against the library
     oic_synth          the synthetic read generator
+    oic_kmers          frequent k-mers of a read container (the -k skip file)
 
 Each translation unit is compiled in parallel; nvcc targets exactly sm_103a.
 """
@@ -27,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
            "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
 CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu", "oic_noalloc.cu",
-              "oic_filter.cu"]
+              "oic_filter.cu", "oic_kmers.cu"]
 
 
 def nvcc():
@@ -88,6 +89,11 @@ def build_tools():
     cli = os.path.join(OUT, "overlapInCore")
     if _stale(cli, [cli_src, lib] + _headers()):
         _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", cli, cli_src, "-L" + OUT, "-loic_gpu",
+              "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
+    km_src = os.path.join(HERE, "host", "oic_kmers.cpp")
+    km = os.path.join(OUT, "oic_kmers")
+    if _stale(km, [km_src, lib] + _headers()):
+        _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", km, km_src, "-L" + OUT, "-loic_gpu",
               "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
     syn_src = os.path.join(HERE, "synth", "oic_synth.cpp")
     syn = os.path.join(OUT, "oic_synth")

@@ -1725,6 +1725,87 @@ int oic_extend_batch(oic_ctx *ctx, uint32_t nAlign, const uint32_t *sRead, const
   return rc;
 }
 
+int oic_count_kmers(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t minCount, char *kmers, uint32_t *counts,
+                    uint64_t maxKmers, uint64_t *nKmers) {
+  if (!ctx || !nKmers || (maxKmers && (!kmers || !counts))) return OIC_ERR_ARG;
+  if (ctx->nReads == 0) return fail(ctx, OIC_ERR_STATE, "no reads loaded");
+  cudaSetDevice(ctx->device);
+  const int K = (int)ctx->P.kmerLen;
+  if (bgnID < 1) bgnID = 1;
+  if (endID > ctx->nReads) endID = ctx->nReads;
+  std::vector<uint32_t> reads;
+  std::vector<uint64_t> flat(1, 0);
+  for (uint64_t id = bgnID; id <= endID; id++) {
+    const uint32_t r = (uint32_t)id - 1;
+    if (ctx->len[r] < (uint32_t)K) continue;
+    reads.push_back(r);
+    flat.push_back(flat.back() + ctx->len[r] - K + 1);
+  }
+  const uint64_t n = flat.back();
+  *nKmers          = 0;
+  if (n == 0) return OIC_OK;
+  if (n >= 0xfffffffeull) return fail(ctx, OIC_ERR_OVERFLOW, "more than 2^32-2 k-mer windows");
+  DevBuf dReads, dFlat, dK, dV, dK2, dV2, dScr, dFlags, dPos, dRun, dSel, dSelPos, dOutK, dOutC;
+  auto release = [&]() {
+    for (DevBuf *b : {&dReads, &dFlat, &dK, &dV, &dK2, &dV2, &dScr, &dFlags, &dPos, &dRun, &dSel, &dSelPos, &dOutK, &dOutC})
+      b->release();
+  };
+  int rc = OIC_OK;
+  auto step = [&](cudaError_t e) {
+    if (e != cudaSuccess && !rc) rc = fail(ctx, OIC_ERR_CUDA, "k-mer count: %s", cudaGetErrorString(e));
+    return rc == OIC_OK;
+  };
+  const size_t nr = reads.size();
+  if (step(dReads.ensure(nr * 4)) && step(dFlat.ensure((nr + 1) * 8)) && step(dK.ensure(n * 8)) && step(dV.ensure(n * 4)) &&
+      step(dK2.ensure(n * 8)) && step(dV2.ensure(n * 4)) &&
+      step(dScr.ensure(std::max(radix_sort_scratch(n), scan_u32_scratch(n)) + 256)) && step(dFlags.ensure(n * 4)) &&
+      step(dPos.ensure(n * 4)) && step(cudaMemcpyAsync(dReads.p, reads.data(), nr * 4, cudaMemcpyHostToDevice, ctx->st)) &&
+      step(cudaMemcpyAsync(dFlat.p, flat.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, ctx->st)) &&
+      step(cudaMemsetAsync(ctr64(ctx) + kCellsSnap, 0, 8, ctx->st))) {
+    launch_canon_emit(ctx->R, dReads.as<uint32_t>(), (uint32_t)nr, dFlat.as<u64>(), K, dK.as<u64>(), dV.as<uint32_t>(),
+                      ctr64(ctx) + kCellsSnap, ctx->st);
+    step(radix_sort_u64_u32(dK.as<u64>(), dV.as<uint32_t>(), dK2.as<u64>(), dV2.as<uint32_t>(), n, 2 * K + 1, dScr.p,
+                            ctx->st));
+  }
+  unsigned long long nInvalid = 0;
+  if (!rc && step(cudaMemcpyAsync(&nInvalid, ctr64(ctx) + kCellsSnap, 8, cudaMemcpyDeviceToHost, ctx->st)))
+    rc = sync_check(ctx, "k-mer sort");
+  const uint64_t nValid = n - nInvalid;   // invalid keys sort last
+  uint32_t       nRuns = 0, nSel = 0;
+  if (!rc && nValid) {
+    launch_run_starts(dK.as<u64>(), nValid, dFlags.as<uint32_t>(), ctx->st);
+    if (step(scan_u32(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nValid, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) &&
+        step(cudaMemcpyAsync(&nRuns, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)))
+      rc = sync_check(ctx, "k-mer runs");
+    if (!rc && step(dRun.ensure((size_t)nRuns * 8 + 8)) && step(dSel.ensure((size_t)nRuns * 4 + 4)) &&
+        step(dSelPos.ensure((size_t)nRuns * 4 + 4))) {
+      launch_run_index(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nValid, dRun.as<u64>(), ctx->st);
+      launch_run_select(dRun.as<u64>(), nRuns, nValid, minCount, dSel.as<uint32_t>(), ctx->st);
+      if (step(scan_u32(dSel.as<uint32_t>(), dSelPos.as<uint32_t>(), nRuns, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) &&
+          step(cudaMemcpyAsync(&nSel, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)))
+        rc = sync_check(ctx, "k-mer selection");
+    }
+  }
+  if (!rc && nSel) {
+    *nKmers = nSel;
+    if (nSel > maxKmers) rc = fail(ctx, OIC_ERR_OVERFLOW, "%u k-mers found, room for %lu", nSel, (unsigned long)maxKmers);
+    else if (step(dOutK.ensure((size_t)nSel * 8)) && step(dOutC.ensure((size_t)nSel * 4))) {
+      launch_run_compact(dK.as<u64>(), dRun.as<u64>(), nRuns, nValid, dSel.as<uint32_t>(), dSelPos.as<uint32_t>(),
+                         dOutK.as<u64>(), dOutC.as<uint32_t>(), ctx->st);
+      std::vector<uint64_t> keys(nSel);
+      if (step(cudaMemcpyAsync(keys.data(), dOutK.p, (size_t)nSel * 8, cudaMemcpyDeviceToHost, ctx->st)) &&
+          step(cudaMemcpyAsync(counts, dOutC.p, (size_t)nSel * 4, cudaMemcpyDeviceToHost, ctx->st)) &&
+          !(rc = sync_check(ctx, "k-mer output"))) {
+        static const char acgt[4] = {'A', 'C', 'G', 'T'};
+        for (uint32_t i = 0; i < nSel; i++)
+          for (int b = 0; b < K; b++) kmers[(size_t)i * K + b] = acgt[(keys[i] >> (2 * b)) & 3];
+      }
+    }
+  }
+  release();
+  return rc;
+}
+
 int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t) {
   if (!ctx) return OIC_ERR_ARG;
   if (!t) {

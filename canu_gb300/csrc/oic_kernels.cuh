@@ -158,6 +158,15 @@ cudaError_t launch_mlp_forward(const void *prm, const void *X, u32 n, float *log
 void launch_list_keys(const PairRec *pairs, const u32 *list, u32 n, unsigned long long *keys, u32 *vals,
                       cudaStream_t st);
 
+// ---------------- frequent k-mers (oic_kmers.cu) ----------------
+void launch_canon_emit(ReadsDev R, const u32 *reads, u32 nReads, const u64 *flatStart, int K, u64 *keys, u32 *vals,
+                       unsigned long long *nInvalid, cudaStream_t st);
+void launch_run_starts(const u64 *keys, u64 nValid, u32 *flags, cudaStream_t st);
+void launch_run_index(const u32 *flags, const u32 *pos, u64 nValid, u64 *runStart, cudaStream_t st);
+void launch_run_select(const u64 *runStart, u32 nRuns, u64 nValid, u32 minCount, u32 *sel, cudaStream_t st);
+void launch_run_compact(const u64 *keys, const u64 *runStart, u32 nRuns, u64 nValid, const u32 *sel, const u32 *pos,
+                        u64 *outKey, u32 *outCount, cudaStream_t st);
+
 // Compact per-pair record slots into a dense record array.
 void launch_compact_records(const u32 *rec, const u32 *cnt, const u32 *pos, u32 nPairs, u32 *dst, cudaStream_t st);
 

@@ -278,6 +278,17 @@ int oic_get_tuning(oic_ctx *ctx, oic_tuning *t);          /* the configuration i
 int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *report, uint32_t maxReport,
                  uint32_t *nReport);
 
+/* Frequent k-mers of reads [bgnID, endID]: the counting step that makes overlapInCore's
+ * -k skip file (in canu: `meryl count` + `meryl print` of the k-mers at or above a
+ * threshold, src/pipelines/canu/Meryl.pm; read back by Build_Hash_Index.C:203-246).
+ * A k-mer and its reverse complement count as one (canonical) k-mer; windows with an N
+ * are skipped.  Writes up to maxKmers k-mers with count >= minCount -- kmerLen bases
+ * each (ACGT), concatenated -- and their counts (saturating at 2^32-1), in ascending
+ * order of the canonical 2-bit key; *nKmers gets the number found (larger than
+ * maxKmers: OIC_ERR_OVERFLOW, call again with room).  At most 2^32-2 windows. */
+int oic_count_kmers(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t minCount, char *kmers, uint32_t *counts,
+                    uint64_t maxKmers, uint64_t *nKmers);
+
 /* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
  * min(n, table length) entries; *len gets the table length. */
 int oic_get_match_limit(oic_ctx *ctx, int32_t *dst, uint32_t n, uint32_t *len);
