@@ -50,6 +50,8 @@ WORKLOAD_TEXT = {
     "c1": ("c1: 5 Mbp iid genome, 20x lognormal reads (8+-3 kb, 1-30 kb), 2% errors 1:1:1; k=22, --minlength 500, "
            "--maxerate 0.06, --hashbits 23"),
     "c3": ("c3: 20 Mbp iid genome, 25x Pareto reads (alpha 1.5, 0.5-100 kb), 5% errors 1:2:2; --maxerate 0.12"),
+    "c5": ("c5: 200 Mbp genome with 1000 x 6 kb repeat copies and 3% tandem arrays; 40x c2-like reads; --hashbits 27, "
+           "--hashdatalen 2e9 (4 hash blocks); frequent-k-mer skip list"),
 }
 
 # Nominal INT32 lanes per SM (Blackwell: 128 unified FP32/INT32 lanes).
@@ -130,6 +132,20 @@ def barrier_max(value, ws, device="cuda"):
     t = torch.tensor([value], dtype=torch.float64, device=device)
     td.all_reduce(t, op=td.ReduceOp.MAX)
     return float(t.item())
+
+
+def dp_bins(res):
+    """Per-bin DP figures of the timed steps (mean over steps): the one-warp bin and the
+    CTA bin (its pairs include the one-warp bin's reruns)."""
+    def mean(k):
+        return statistics.mean(float(r[0].get(k, 0)) for r in res)
+    cells_all, cells_wide = mean("dpCells"), mean("cellsWide")
+    out = {}
+    for name, pairs, ms, cells in (("one_warp", mean("pairsNarrow"), mean("msNarrow"), cells_all - cells_wide),
+                                   ("cta", mean("pairsWide"), mean("msWide"), cells_wide)):
+        out[name] = {"pairs": pairs, "ms": ms, "dp_cells": cells,
+                     "dp_cells_per_sec": cells / (ms / 1000.0) if ms > 0 else None}
+    return out
 
 
 def replica_rate(units_per_rank, seconds, ws, device="cuda"):
@@ -245,7 +261,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c5"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--data-dir", default=os.environ.get("OIC_BENCH_DATA", "/tmp/oic_bench"))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -407,6 +423,7 @@ def main():
                  "dp_cells": cells, "dp_rows": st0.get("dpRows"), "slide_bases": slides,
                  "ms_hash": statistics.mean(r[0]["msHash"] for r in res),
                  "ms_seed": statistics.mean(r[0]["msSeed"] for r in res), "ms_align": ms_align},
+        "dp_bins": dp_bins(res),
         "e2e": {"value": e2e, "unit": "overlaps/s", "h2d_bytes_per_step": int(host_bases.nbytes + ln.nbytes * 3 + off.nbytes),
                 "d2h_bytes_per_step": int(n_ov * 24), "pinned": pinned_ok, "timing": "wall clock"},
         "roofline": {"bound": "hbm", "kernel": "align_kernel", "achieved": achieved,
