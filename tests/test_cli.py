@@ -38,3 +38,24 @@ def test_bad_gpu_tune_is_rejected(built, tmp_path, tune):
 def test_missing_store_is_reported(built, tmp_path):
     r = run(built, "-k", "22", "-o", str(tmp_path / "o.ovb"), str(tmp_path / "no_such.seqdb"))
     assert r.returncode == 1 and "Failed to load read container" in r.stderr
+
+
+@pytest.mark.parametrize("damage", ["magic", "truncated_index", "truncated_bases", "offset_out_of_range"])
+def test_malformed_read_container_is_rejected(built, tmp_path, damage):
+    import struct
+    import canu_gb300 as oic
+    db = str(tmp_path / "in.seqdb")
+    oic.write_seqdb(db, ["ACGT" * 300, "TTGCA" * 200])
+    raw = bytearray(open(db, "rb").read())
+    hdr = 8 + 4 + 4 + 8
+    if damage == "magic":
+        raw[0:8] = b"NOTSEQ01"
+    elif damage == "truncated_index":
+        raw = raw[:hdr + 10]
+    elif damage == "truncated_bases":
+        raw = raw[:-7]
+    else:   # second read's offset pushed past the bases
+        struct.pack_into("<Q", raw, hdr + 16 + 8, 10**9)
+    open(db, "wb").write(bytes(raw))
+    r = run(built, "-k", "22", "-o", str(tmp_path / "o.ovb"), db)
+    assert r.returncode == 1 and "Failed to load read container" in r.stderr
