@@ -260,25 +260,35 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0
   // Row buffers hold diagonal d at index d - base + 2.  Before a row is computed the
   // two diagonals on each side of the previous row's kept band are set to -2, as the
   // reference does (forward.C:150-153), so the neighbour reads need no bounds tests.
+  // Loop invariants and the slide counter in registers: the loop stores through
+  // generic pointers, which the compiler cannot tell apart from the WarpDP on the stack.
+  int *const         arena    = w.sc.arena;
+  int4 *const        rowHdr   = w.sc.rowHdr;
+  int *const         rowsG    = w.sc.rowsG;
+  const int *const   eml      = w.eml;
+  const int          rowCap   = w.cap.rowCap;
+  const int          rowsGW   = w.cap.rowsGW;
+  const int          arenaCap = w.cap.arenaCap;
+  unsigned long long slides   = 0;
   int *prev = w.smA, *cur = w.smB;
   int  bufW = w.cap.bandW;
   int  used = 1, prevBase = 0, L = 0, R = 0;
   for (int e = 1; e <= errorLimit; e++) {
-    if (e >= w.cap.rowCap) { o.status = kRowsErr; o.err = kErrRowsFull; break; }
+    if (e >= rowCap) { o.status = kRowsErr; o.err = kErrRowsFull; break; }
     const int Lc = max(L - 1, -e), Rc = min(R + 1, e);
     const int width = Rc - Lc + 1;
     if (width + 4 > bufW) {
       // The band outgrew the shared-memory rows: continue in the warp's HBM rows.
-      if (bufW == w.cap.rowsGW || width + 4 > w.cap.rowsGW || !w.sc.rowsG) { o.status = kRowsErr; o.err = kErrBandWide; break; }
-      int *gA = w.sc.rowsG, *gB = w.sc.rowsG + w.cap.rowsGW;
+      if (bufW == rowsGW || width + 4 > rowsGW || !rowsG) { o.status = kRowsErr; o.err = kErrBandWide; break; }
+      int *gA = rowsG, *gB = rowsG + rowsGW;
       for (int i = lane; i < bufW; i += 32) gA[i] = prev[i];
       __syncwarp();
       prev = gA;
       cur  = gB;
-      bufW = w.cap.rowsGW;
+      bufW = rowsGW;
     }
 
-    const int lim = w.eml[e];
+    const int lim = eml[e];
     if (lane < 4) prev[(lane < 2 ? L - 2 + lane : R - 1 + lane) - prevBase + 2] = -2;
     __syncwarp();
     const int *pv = prev + (2 - prevBase);   // pv[d] = row e-1 at diagonal d
@@ -290,7 +300,7 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0
       if (pm > row) row = pm;
       if (1 + pp > row) row = 1 + pp;
       const int room = min(m - row, n - row - d);
-      if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, w.slides);
+      if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, slides);
       cv[d] = row;
       if ((row == m || row + d == n) && d < myEnd) myEnd = d;
       // pruneAlign (prefixEditDistance.H:249-258): extra = max(d, 0) on both band edges
@@ -325,15 +335,15 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0
     // (forward.C:284-289); the Max_Score test that uses it runs once after the rows
     // (max_score_rows).
     const int cnt = R2 - L2 + 1;
-    if (used + cnt > w.cap.arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
+    if (used + cnt > arenaCap) { o.status = kRowsErr; o.err = kErrArenaFull; break; }
     int myV = -1;
     for (int d = L2 + lane; d <= R2; d += 32) {
       const int v = cv[d];
       myV         = max(myV, v);
-      w.sc.arena[used + d - L2] = v;
+      arena[used + d - L2] = v;
     }
     const int rowMax = __reduce_max_sync(0xffffffffu, myV);
-    if (lane == 0) w.sc.rowHdr[e] = make_int4(used, L2, R2, rowMax);
+    if (lane == 0) rowHdr[e] = make_int4(used, L2, R2, rowMax);
     used += cnt;
     int *t = prev;
     prev   = cur;
@@ -344,6 +354,7 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0
     o.eDone  = e;
     __syncwarp();
   }
+  w.slides += slides;
   return o;
 }
 
