@@ -89,14 +89,21 @@ __device__ __forceinline__ int warp_slide0(const SeqView &A, i64 a0, const SeqVi
 // Traceback of Set_Right_Delta / Set_Left_Delta (prefixEditDistance-forward.C:32-71,
 // -reverse.C:36-93) from row e, diagonal d whose value is `last`.  Lane 0 only.
 // Pushes one entry per indel into out[]; returns the value reached on row 0.
-static __device__ __noinline__ int trace_rows(const WarpDP &w, int e, int d, int last, int *out, int &n) {
-  n = 0;
+static __device__ __noinline__ int trace_rows(const WarpDP &w, int e, int d, int last, int *out, int &nOut) {
+  // Pointers and the entry count in registers; the next row's header is loaded one
+  // step ahead (it does not depend on the path), so only the arena reads stay on the
+  // step-to-step dependency chain.
+  const int4 *const rowHdr = w.sc.rowHdr;
+  const int *const  arena  = w.sc.arena;
+  int  n     = 0;
+  int4 hNext = e > 0 ? rowHdr[e - 1] : make_int4(0, 0, 0, 0);
   for (int k = e; k > 0; k--) {
-    const int4 h = w.sc.rowHdr[k - 1];
+    const int4 h = hNext;
+    if (k > 1) hNext = rowHdr[k - 2];
     const int off = h.x, L = h.y, R = h.z;
-    const int g0 = (d >= L && d <= R) ? w.sc.arena[off + d - L] : -2;
-    const int gm = (d - 1 >= L && d - 1 <= R) ? w.sc.arena[off + d - 1 - L] : -2;
-    const int gp = (d + 1 >= L && d + 1 <= R) ? w.sc.arena[off + d + 1 - L] : -2;
+    const int g0 = (d >= L && d <= R) ? arena[off + d - L] : -2;
+    const int gm = (d - 1 >= L && d - 1 <= R) ? arena[off + d - 1 - L] : -2;
+    const int gp = (d + 1 >= L && d + 1 <= R) ? arena[off + d + 1 - L] : -2;
     int from = d, mx = 1 + g0;
     if (gm > mx) { from = d - 1; mx = gm; }
     if (1 + gp > mx) { from = d + 1; mx = 1 + gp; }
@@ -110,6 +117,7 @@ static __device__ __noinline__ int trace_rows(const WarpDP &w, int e, int d, int
       d++;
     }
   }
+  nOut = n;
   return last;
 }
 
