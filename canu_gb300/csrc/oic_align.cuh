@@ -257,8 +257,9 @@ __device__ __forceinline__ void group_bar(int id, int nThr) {
 
 // The row loop by one warp.  Row 0 (value r0) is in prev[2].
 template <int STEP>
-__device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0,
-                                             int n, int errorLimit) {
+__device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, i64 a0, int m, const SeqView &Tref,
+                                             i64 t0, int n, int errorLimit) {
+  const SeqView A = Aref, T = Tref;   // in registers for the slides
   const int lane = threadIdx.x & 31;
   RowsOut o;
   o.status = kRowsDone;
@@ -376,6 +377,9 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
                                                   const int *eml, int tid, int nThr, int (*red)[4],
                                                   unsigned long long &slides) {
   const int lane = tid & 31, wid = tid >> 5, nW = nThr >> 5;
+  const SeqView A = j.A, T = j.T;   // in registers for the slides
+  const i64     a0 = j.a0, t0 = j.t0;
+  const int     m = j.m, n = j.n;
   RowsOut o;
   o.status = kRowsDone;
   o.err = 0;
@@ -416,10 +420,10 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
           int row = 1 + q[k + 1];
           if (q[k] > row) row = q[k];
           if (1 + q[k + 2] > row) row = 1 + q[k + 2];
-          const int room = min(j.m - row, j.n - row - d);
-          if (room > 0) row += slide<STEP>(j.A, j.a0, j.T, j.t0, row, d, room, slides);
+          const int room = min(m - row, n - row - d);
+          if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, slides);
           cv[d] = row;
-          if ((row == j.m || row + d == j.n) && d < myEnd) myEnd = d;
+          if ((row == m || row + d == n) && d < myEnd) myEnd = d;
           if (!(row + max(d, 0) < lim)) {
             if (myL == INT_MAX) myL = d;
             myR = d;
