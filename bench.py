@@ -405,9 +405,9 @@ def main():
     alg_bytes = pairs * (32 + 72 + 4 + 2 * mean_len / 4) + nodes * 16
     achieved = alg_bytes / (ms_align / 1000.0) / 1e9
     # DRAM bytes per DP cell of the one-warp DP kernel, from one ncu capture of a 1/50
-    # scale c2 launch (6.39 GB read + 18.58 GB written for 6.598 G cells; the figures and
+    # scale c2 launch (10.73 GB read + 22.65 GB written for 6.598 G cells; the figures and
     # the command are in profiles/align_kernel_c2_scale0.02_ncu.md), scaled to this job.
-    traffic = 3.784 * cells
+    traffic = 5.059 * cells
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
     int_ops = 6 * cells + slides / 16.0
