@@ -32,6 +32,11 @@ EXPORTS = (
     "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam", "oic_set_tuning", "oic_get_tuning",
     "oic_autotune", "oic_count_kmers",
 )
+# Output files (include/oic_ovfile.h): host code of the same library, no GPU needed.
+OVFILE_EXPORTS = (
+    "oic_ovb_write", "oic_ovb_read", "oic_oc_path", "oic_oc_write", "oic_oc_read", "oic_merge_outputs",
+    "oic_snappy_max_length", "oic_snappy_compress", "oic_snappy_uncompress",
+)
 
 # Learned candidate filter (include/oic_gpu.h): feature row width, hidden width and the
 # FP16 parameter array w1[128][80] | b1[128] | w2[128][128] | b2[128] | w3[128] | b3.
@@ -85,6 +90,18 @@ class OicStats(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class FilterDomain(ctypes.Structure):
+    """oic_filter_domain: the parameters a filter network was trained under."""
+    _fields_ = [("kmerLen", ctypes.c_uint32), ("minOlapLen", ctypes.c_int32), ("maxErate", ctypes.c_double)]
+
+
+def filter_domain(params):
+    """The filter domain of an oic_params (or of a dict with kmerLen, minOlapLen, maxErate)."""
+    g = (lambda k: params[k]) if isinstance(params, dict) else (lambda k: getattr(params, k))
+    return {"kmerLen": int(g("kmerLen")), "minOlapLen": int(g("minOlapLen")),
+            "maxErate": float(np.float32(g("maxErate")))}
+
+
 class OicTuning(ctypes.Structure):
     """oic_tuning: DP launch configuration (zeros = defaults)."""
     _fields_ = [("narrowArena", ctypes.c_uint32), ("wideMinLen", ctypes.c_uint32), ("wideThreads", ctypes.c_uint32),
@@ -122,7 +139,17 @@ def library():
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
-        lib.oic_set_filter.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float, U32]
+        lib.oic_ovb_write.argtypes = [ctypes.c_char_p, vp, U64, ctypes.c_int]
+        lib.oic_ovb_read.argtypes = [ctypes.c_char_p, vp, U64, P(U64)]
+        lib.oic_oc_path.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        lib.oic_oc_write.argtypes = [ctypes.c_char_p, vp, U64, U32]
+        lib.oic_oc_read.argtypes = [ctypes.c_char_p, P(U64), vp, U32, P(U32)]
+        lib.oic_merge_outputs.argtypes = [ctypes.c_char_p, P(ctypes.c_char_p), U32]
+        lib.oic_snappy_max_length.restype = ctypes.c_size_t
+        lib.oic_snappy_max_length.argtypes = [ctypes.c_size_t]
+        lib.oic_snappy_compress.argtypes = [vp, ctypes.c_size_t, vp, P(ctypes.c_size_t)]
+        lib.oic_snappy_uncompress.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, P(ctypes.c_size_t)]
+        lib.oic_set_filter.argtypes = [vp, vp, ctypes.c_float, ctypes.c_float, U32, P(FilterDomain)]
         lib.oic_collect_pairs.argtypes = [vp, ctypes.c_int]
         lib.oic_num_pairs.argtypes = [vp, P(U64), P(U64)]
         lib.oic_get_pairs.argtypes = [vp, vp, vp, vp, U64, U64]
@@ -268,18 +295,24 @@ class Overlapper:
         self._check(self._lib.oic_get_match_limit(self._ctx, _ptr(out), n.value, ctypes.byref(n)))
         return out
 
-    def set_filter(self, params, threshold, full_threshold=0.0, ext_budget=1):
+    def set_filter(self, params, threshold, full_threshold=0.0, ext_budget=1, domain=None):
         """Learned candidate filter: params = FILTER_NPARAM float16 values (None: off).
         Pairs scored below threshold are dropped; below full_threshold they stop once
-        ext_budget extensions have found no overlap."""
+        ext_budget extensions have found no overlap.  domain: the parameters the network
+        was trained under (kmerLen, minOlapLen, maxErate; a trained file's
+        meta["domain"]); the library refuses a network trained under other values."""
         if params is None:
-            self._check(self._lib.oic_set_filter(self._ctx, None, 0.0, 0.0, 0))
+            self._check(self._lib.oic_set_filter(self._ctx, None, 0.0, 0.0, 0, None))
             return
         prm = np.ascontiguousarray(params, dtype=np.float16).view(np.uint16)
         if prm.size != FILTER_NPARAM:
             raise ValueError(f"filter needs {FILTER_NPARAM} parameters, got {prm.size}")
+        dom = None
+        if domain is not None:
+            d = filter_domain(domain)
+            dom = FilterDomain(d["kmerLen"], d["minOlapLen"], d["maxErate"])
         self._check(self._lib.oic_set_filter(self._ctx, _ptr(prm), float(threshold), float(full_threshold),
-                                             int(ext_budget)))
+                                             int(ext_budget), ctypes.byref(dom) if dom is not None else None))
 
     def collect_pairs(self, mode=1):
         """0 off, 1 candidate pairs + feature rows, 2 also their match runs."""
@@ -372,6 +405,53 @@ def mlp_adam(master, m, v, grad, params, lr, beta1, beta2, eps, grad_scale, weig
     """oic_mlp_adam on device pointers (ints)."""
     _mlp_check(library().oic_mlp_adam(master, m, v, grad, params, lr, beta1, beta2, eps, grad_scale, weight_decay,
                                       step, stream or None), "mlp adam")
+
+
+def _file_check(rc, what, path):
+    if rc == 1:
+        raise OSError(ctypes.get_errno() or 5, f"{what} failed", path)
+    if rc:
+        raise ValueError(f"{path}: {what}: malformed file or argument")
+
+
+def write_ovb(path, records, framing=1):
+    """Write records ((n, 6) uint32) as canu's ovFile(ovFileFullWrite): snappy blocks
+    (framing 1) or unframed words (framing 0)."""
+    r = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 6)
+    _file_check(library().oic_ovb_write(os.fsencode(path), _ptr(r), len(r), int(framing)), "write .ovb", path)
+
+
+def read_ovb(path):
+    """Records ((n, 6) uint32) of a snappy-framed .ovb file."""
+    lib, n = library(), ctypes.c_uint64()
+    _file_check(lib.oic_ovb_read(os.fsencode(path), None, 0, ctypes.byref(n)), "read .ovb", path)
+    out = np.zeros((n.value, 6), dtype=np.uint32)
+    _file_check(lib.oic_ovb_read(os.fsencode(path), _ptr(out), n.value, ctypes.byref(n)), "read .ovb", path)
+    return out
+
+
+def oc_path(ovb_path):
+    """The .oc name canu pairs with an .ovb name (cut at the first '.' of the file name)."""
+    buf = ctypes.create_string_buffer(4096)
+    _file_check(library().oic_oc_path(os.fsencode(ovb_path), buf, 4096), "oc name", ovb_path)
+    return os.fsdecode(buf.value)
+
+
+def read_oc(path):
+    """(number of records, per-read counts [oprMax] uint32) of an .oc file."""
+    lib, n, m = library(), ctypes.c_uint64(), ctypes.c_uint32()
+    _file_check(lib.oic_oc_read(os.fsencode(path), ctypes.byref(n), None, 0, ctypes.byref(m)), "read .oc", path)
+    opr = np.zeros(m.value, dtype=np.uint32)
+    if m.value:
+        _file_check(lib.oic_oc_read(os.fsencode(path), ctypes.byref(n), _ptr(opr), m.value - 1, ctypes.byref(m)),
+                    "read .oc", path)
+    return n.value, opr
+
+
+def merge_outputs(out_ovb, inputs):
+    """Merge independent jobs' .ovb/.oc outputs into out_ovb and its .oc."""
+    arr = (ctypes.c_char_p * len(inputs))(*[os.fsencode(x) for x in inputs])
+    _file_check(library().oic_merge_outputs(os.fsencode(out_ovb), arr, len(inputs)), "merge", out_ovb)
 
 
 def sort_records(rec):

@@ -8,6 +8,7 @@ Outputs (git-ignored) go to canu_gb300/_build/:
     overlapInCore      the drop-in command line, linked against the library
     oic_synth          the synthetic read generator
     oic_kmers          frequent k-mers of a read container (the -k skip file)
+    oic_merge          merges the outputs of independent jobs (.ovb blocks, .oc counts)
 
 Each translation unit is compiled in parallel; nvcc targets exactly sm_103a.
 """
@@ -29,6 +30,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "
            "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
 CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu", "oic_noalloc.cu",
               "oic_filter.cu", "oic_kmers.cu"]
+HOST_SOURCES = ["oic_ovfile.cpp"]   # canu_gb300/host: host-only parts of the library
 
 
 def nvcc():
@@ -70,7 +72,13 @@ def build_lib(verbose=False, extra=()):
         objs.append(o)
         if _stale(o, [s] + hdrs):
             jobs.append([nv] + ARCH + NVFLAGS + list(extra) + ["-c", s, "-o", o])
-    with ThreadPoolExecutor(max_workers=len(CU_SOURCES)) as ex:
+    for src in HOST_SOURCES:
+        s = os.path.join(HERE, "host", src)
+        o = os.path.join(OUT, src.replace(".cpp", ".o"))
+        objs.append(o)
+        if _stale(o, [s] + hdrs):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out.strip():
                 print(out)
@@ -80,26 +88,35 @@ def build_lib(verbose=False, extra=()):
     return lib
 
 
-def build_tools():
+def build_synth():
+    """The synthetic read generator (host only; no CUDA)."""
     os.makedirs(OUT, exist_ok=True)
-    nv = nvcc()
-    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
-    lib = os.path.join(OUT, "liboic_gpu.so")
-    cli_src = os.path.join(HERE, "host", "overlapInCore.cpp")
-    cli = os.path.join(OUT, "overlapInCore")
-    if _stale(cli, [cli_src, lib] + _headers()):
-        _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", cli, cli_src, "-L" + OUT, "-loic_gpu",
-              "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
-    km_src = os.path.join(HERE, "host", "oic_kmers.cpp")
-    km = os.path.join(OUT, "oic_kmers")
-    if _stale(km, [km_src, lib] + _headers()):
-        _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", km, km_src, "-L" + OUT, "-loic_gpu",
-              "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
     syn_src = os.path.join(HERE, "synth", "oic_synth.cpp")
     syn = os.path.join(OUT, "oic_synth")
     if _stale(syn, [syn_src, os.path.join(INC, "oic_seqdb.h")]):
         _run(["g++", "-O2", "-std=c++17", "-I" + INC, "-o", syn, syn_src])
-    return cli, syn
+    return syn
+
+
+def build_tools():
+    """The command-line tools, linked against liboic_gpu.so: overlapInCore (the drop-in),
+    oic_kmers (frequent k-mers) and oic_merge (merges independent jobs' outputs)."""
+    os.makedirs(OUT, exist_ok=True)
+    nv = nvcc()
+    cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
+    lib = os.path.join(OUT, "liboic_gpu.so")
+    tools = {"overlapInCore": "overlapInCore.cpp", "oic_kmers": "oic_kmers.cpp", "oic_merge": "oic_merge.cpp"}
+    jobs = []
+    for name, src in tools.items():
+        s = os.path.join(HERE, "host", src)
+        t = os.path.join(OUT, name)
+        if _stale(t, [s, lib] + _headers()):
+            jobs.append(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INC, "-o", t, s, "-L" + OUT, "-loic_gpu",
+                         "-Wl,-rpath,$ORIGIN", "-L" + os.path.join(cuda_home, "lib64"), "-lcudart"])
+    with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
+        list(ex.map(_run, jobs))
+    syn = build_synth()
+    return os.path.join(OUT, "overlapInCore"), syn
 
 
 def main(argv=None):

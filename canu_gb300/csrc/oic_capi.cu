@@ -191,6 +191,8 @@ constexpr int kSeedStatBase  = 16;   // u64 index: [seeds, segments]
 constexpr int kAlignStatBase = 20;   // u64 index: kStCount entries
 constexpr int kExtStatBase   = 40;
 constexpr int kCellsSnap     = 60;   // u64 index: DP cells after the one-warp bin of a captured batch
+static_assert(kNoAllocStatBase >= kExtStatBase + 3 && kNoAllocStatBase + 3 <= kCellsSnap,
+              "the no-allocation entry point's counters overlap another slot");
 
 uint32_t *ctr32(oic_ctx *c) { return c->dCtr.as<uint32_t>(); }
 unsigned long long *ctr64(oic_ctx *c) { return (unsigned long long *)c->dCtr.as<uint32_t>(); }
@@ -1027,6 +1029,12 @@ void ctx_set_error(oic_ctx *ctx, const char *msg) {
   if (ctx) ctx->lastErr = msg;
 }
 
+void ctx_add_dp_work(oic_ctx *ctx, unsigned long long cells, unsigned long long slides) {
+  if (!ctx) return;
+  ctx->stats.dpCells += cells;
+  ctx->stats.slideBases += slides;
+}
+
 }  // namespace oic
 
 // =================================================================================
@@ -1549,12 +1557,21 @@ int oic_get_stats(oic_ctx *ctx, oic_stats *st) {
   return OIC_OK;
 }
 
-int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold, uint32_t extBudget) {
+int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold, uint32_t extBudget,
+                   const oic_filter_domain *trainedOn) {
   if (!ctx) return OIC_ERR_ARG;
   if (!params) {
     ctx->filterOn = false;
     return OIC_OK;
   }
+  if (!trainedOn) return fail(ctx, OIC_ERR_ARG, "a filter needs the parameters it was trained under");
+  if (trainedOn->kmerLen != ctx->P.kmerLen || trainedOn->minOlapLen != ctx->P.minOlapLen ||
+      (float)trainedOn->maxErate != (float)ctx->P.maxErate)
+    return fail(ctx, OIC_ERR_ARG,
+                "the filter was trained for -k %u --minlength %d --maxerate %g; this context runs -k %u "
+                "--minlength %d --maxerate %g",
+                trainedOn->kmerLen, trainedOn->minOlapLen, (double)(float)trainedOn->maxErate, ctx->P.kmerLen,
+                ctx->P.minOlapLen, (double)(float)ctx->P.maxErate);
   if (!(threshold >= 0.0f && threshold < 1.0f) || !(fullThreshold >= 0.0f && fullThreshold < 1.0f))
     return fail(ctx, OIC_ERR_ARG, "filter thresholds must be in [0, 1)");
   cudaSetDevice(ctx->device);

@@ -1,24 +1,32 @@
 // oic_noalloc.cu -- batched Extend_Alignment for callers that cannot allocate GPU memory.
 //
 // Some callers of this library cannot call cudaMalloc at the point where they want to
-// align: code running while a CUDA stream is being captured into a graph, allocators
-// that own the whole device pool, or plugins that were given a fixed memory budget.
-// For them, oic_extend_batch_noalloc() runs the same warp DP as oic_extend_batch() on
-// problems and outputs the caller already holds in device memory, and keeps the DP's
-// working rows, traceback arena and delta lists in one file-scope device array
-// (g_dpScratch, kScratchBytes bytes).  Every GPU that loads the library holds that
-// array until the process exits.  The entry point itself calls no cudaMalloc, no
-// cudaFree and no allocating library routine.
+// align: programs whose own allocator has reserved the whole device memory pool up
+// front (a cudaMalloc from the library would then fail or fragment that pool), and
+// plugins that were handed a fixed device-memory budget by their host application and
+// must not grow it.  For them, oic_extend_batch_noalloc() runs the same warp DP as
+// oic_extend_batch() on problems and outputs the caller already holds in device
+// memory, and keeps the DP's working rows, traceback arena and delta lists in one
+// file-scope device array (g_dpScratch, kScratchBytes bytes).  Every GPU that loads
+// the library holds that array until the process exits.  The entry point itself calls
+// no cudaMalloc, no cudaFree and no allocating library routine.
 //
 // Limits, fixed by the array: 32 warps share it, and each problem may keep at most
 // 131072 DP cells and 8191 error rows on each side of its seed match.  A problem that
 // needs more gets a nonzero status and the call returns OIC_ERR_OVERFLOW; the
 // allocating oic_extend_batch() handles such problems.
 //
+// Set-up: the first call on a device, with that device current, looks up the array's
+// device address with cudaGetSymbolAddress and keeps it for later calls on that device
+// (host code cannot use the symbol itself: on the host it names a stand-in, not device
+// memory).  Make that first call before any stream capture.  A cudaDeviceReset() ends
+// the context the address belongs to; a process that resets a device must not call
+// this entry point on that device afterwards.
+//
 // The array is shared by every call and keeps the previous call's contents; the DP
-// writes each cell before it reads it, so nothing needs clearing between calls.  Calls
-// that overlap on the GPU (two streams, or two host threads) race on the array and
-// must be serialised by the caller.
+// writes each cell before it reads it, so nothing needs clearing between calls, and
+// the call clears its own counters.  Calls that overlap on the GPU (two streams, or two
+// host threads) race on the array and must be serialised by the caller.
 #include <mutex>
 
 #include "oic_gpu.h"
@@ -92,20 +100,22 @@ extern "C" int oic_extend_batch_noalloc(oic_ctx *ctx, uint32_t nAlign, const oic
   cap.rowsGW   = kNaBandW;
 
   // Counters in the context's preallocated block: [cells, slides, error flags].
-  unsigned long long *stats = (unsigned long long *)v.ctr32 + 48;
+  unsigned long long *stats = (unsigned long long *)v.ctr32 + kNoAllocStatBase;
   if (cudaMemsetAsync(stats, 0, 3 * sizeof(unsigned long long), v.st) != cudaSuccess) return OIC_ERR_CUDA;
   constexpr int wpb = 8;
   extend_batch_kernel<kNaBandW, wpb, true><<<kNaWarps / wpb, wpb * 32, (size_t)wpb * 2 * kNaBandW * sizeof(int), v.st>>>(
       v.R, v.dp, v.eml, (const ExtendProblem *)dProblems, nAlign, sc, cap, dOut, dKind, dDeltaLen, dStatus, stats);
   g_launches++;
-  uint32_t flags = 0;
-  cudaError_t e = cudaMemcpyAsync(&flags, stats + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, v.st);
+  unsigned long long counters[3] = {0, 0, 0};
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counters, stats, sizeof(counters), cudaMemcpyDeviceToHost, v.st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(v.st);
-  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     ctx_set_error(ctx, cudaGetErrorString(e));
     return OIC_ERR_CUDA;
   }
+  ctx_add_dp_work(ctx, counters[0], counters[1]);
+  const uint32_t flags = (uint32_t)counters[2];
   if (flags & kErrInternal) {
     ctx_set_error(ctx, "a problem names a read outside the store or a match outside its reads");
     return OIC_ERR_ARG;

@@ -51,15 +51,17 @@ def init_params(seed=0):
 
 
 def run_workload(name, seed, scale, workdir, device=0, collect=0, params=None, threshold=0.0, full_threshold=0.0,
-                 ext_budget=1):
-    """One whole job of a workload: (records, stats, pairs info, feature rows)."""
+                 ext_budget=1, domain=None):
+    """One whole job of a workload: (records, stats, pairs info, feature rows).  domain:
+    the parameters the network was trained under (default: this workload's own)."""
     db, skip = workloads.generate(name, workdir, scale=scale, seed=seed)
     with Overlapper(workloads.params(name), device) as ov:
         ov.set_reads_seqdb(db)
         if skip:
             ov.set_skip_kmers(workloads.read_skip(skip))
         if params is not None:
-            ov.set_filter(params, threshold, full_threshold, ext_budget)
+            ov.set_filter(params, threshold, full_threshold, ext_budget,
+                          domain=domain if domain is not None else training_domain(name))
         if collect:
             ov.collect_pairs(collect)
         ov.run()
@@ -67,6 +69,18 @@ def run_workload(name, seed, scale, workdir, device=0, collect=0, params=None, t
         st = ov.stats()
         info, feat = ov.pairs() if collect else (None, None)
     return recs, st, info, feat
+
+
+def training_domain(name):
+    """The filter domain of a workload: the overlapInCore parameters its network sees."""
+    from . import filter_domain
+    return filter_domain(workloads.WORKLOADS[name]["params"])
+
+
+def read_errors(name):
+    """The read error regime a workload's reads are generated with."""
+    sy = workloads.WORKLOADS[name]["synth"]
+    return f"{100 * sy['err']:g}% errors, sub:ins:del {sy['ratio']}"
 
 
 def sample_weights(info, pos_weight=4.0):
@@ -234,14 +248,16 @@ def compare(plain, filt):
 
 
 def evaluate(params, threshold, name="c2", seed=6, scale=1.0, workdir="/tmp/oic_filter", device=0,
-             full_threshold=None, budget=1, pairs=True):
+             full_threshold=None, budget=1, pairs=True, domain=None):
     """Plain vs filtered run of one read set; returns a dict of the measured figures.
-    pairs=False skips the pair-level figures (a third run collecting every pair)."""
+    pairs=False skips the pair-level figures (a third run collecting every pair).
+    domain: the parameters the network was trained under (default: the workload's)."""
     if full_threshold is None:
         full_threshold = threshold
     out = {}
     if pairs:
-        _, _, info, _ = run_workload(name, seed, scale, workdir, device, collect=1, params=params, threshold=0.0)
+        _, _, info, _ = run_workload(name, seed, scale, workdir, device, collect=1, params=params, threshold=0.0,
+                                     domain=domain)
         y = info["overlaps"] > 0
         rec_replay, _, kept = policy_cost(info, info["score"], threshold, full_threshold, budget)
         keep = ~(info["score"] < np.float32(_logit(threshold)))
@@ -254,7 +270,7 @@ def evaluate(params, threshold, name="c2", seed=6, scale=1.0, workdir="/tmp/oic_
         del info
     rp, sp, _, _ = run_workload(name, seed, scale, workdir, device)
     rf, sf, _, _ = run_workload(name, seed, scale, workdir, device, params=params, threshold=threshold,
-                                full_threshold=full_threshold, ext_budget=budget)
+                                full_threshold=full_threshold, ext_budget=budget, domain=domain)
     recall, exact = compare(rp, rf)
     mk = lambda recs, s: {
         "overlaps": int(len(recs)), "ms": s["msTotal"], "ms_align": s["msAlign"], "dp_cells": int(s["dpCells"]),
@@ -278,9 +294,13 @@ def save(path, params, threshold, full_threshold, meta, budget=1):
 
 def load(path):
     """(params float16[FILTER_NPARAM], drop threshold, full threshold, meta dict); the
-    extension budget is meta["budget"]."""
+    extension budget is meta["budget"], the parameters the network was trained under
+    meta["domain"] (kmerLen, minOlapLen, maxErate) and the training reads' error regime
+    meta["read_errors"]."""
     z = np.load(path)
     meta = json.loads(str(z["meta"]))
+    if "domain" not in meta:
+        raise ValueError(f"{path}: the filter file does not name the parameters it was trained under")
     meta["budget"] = int(z["budget"]) if "budget" in z else 1
     return z["params"].astype(np.float16), float(z["threshold"]), float(z["full_threshold"]), meta
 
@@ -348,7 +368,8 @@ def main(argv=None):
             "train_seconds": train_s, "train_samples_per_s": n * a.epochs / train_s,
             "train_tflops": flops / train_s / 1e12, "train_recall_replayed": rec_tr,
             "train_cells_left_frac": cost_tr / float(info["cells"].astype(np.float64).sum()),
-            "train_pairs_kept": kept_tr, "budget": a.budget}
+            "train_pairs_kept": kept_tr, "budget": a.budget, "domain": training_domain(a.workload),
+            "read_errors": read_errors(a.workload)}
     log(f"thresholds: drop {thr:.6g}, full {full:.6g}; training replay: recall {rec_tr:.5f}, "
         f"cells left {meta['train_cells_left_frac']:.4f}, pairs kept {kept_tr}")
     if a.out:

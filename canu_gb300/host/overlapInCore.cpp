@@ -1,16 +1,20 @@
 // overlapInCore -- drop-in command line for canu's overlap stage on one GB300.
 //
 // Takes the reference's command line (overlapInCore.C:283-450) and writes what it
-// writes: the overlap records of ovFile(ovFileFullWrite) (ovStoreFile.C:212-286) to -o,
-// the <prefix>.oc per-read counts (ovStoreFile.H:50-115) and the -s stats file
-// (overlapInCore.C:539-560).  All overlap computation happens in liboic_gpu.so.
+// writes: the overlap records of ovFile(ovFileFullWrite) -- snappy-compressed blocks,
+// ovStoreFile.C:212-286 -- to -o, the <prefix>.oc per-read counts (ovStoreFile.H:50-115)
+// and the -s stats file (overlapInCore.C:539-560).  All overlap computation happens in
+// liboic_gpu.so; the files are written by its oic_ovfile.h functions.  The output files
+// are opened before any work starts, as the reference opens its ovFile
+// (overlapInCore.C:169), and a failed open, write or close exits with status 1, so a
+// pipeline that renames the output only after success never sees a partial file.
 //
 // Differences from the reference command line:
 //   * the positional store argument is an oic_seqdb read container (include/oic_seqdb.h);
 //   * -l <n> (a per-read overlap cap that makes read pairs depend on each other) is
 //     rejected;
-//   * --gpu-device <d> picks the CUDA device, --ovb-snappy frames the records in snappy
-//     blocks as ovFile does (default: the six-word records unframed);
+//   * --gpu-device <d> picks the CUDA device; --ovb-raw writes the six-word records
+//     unframed instead of in snappy blocks (--ovb-snappy, the default, is accepted);
 //   * --gpu-tune key=value[,key=value...] sets DP launch fields of oic_tuning
 //     (narrowArena, wideMinLen, wideThreads, wideTile, wideBandW, wideCtas, wideArena,
 //     forceWide, noGraph), and --gpu-autotune <n> times the DP grid on the first n ref reads
@@ -27,6 +31,7 @@
 #include <vector>
 
 #include "oic_gpu.h"
+#include "oic_ovfile.h"
 #include "oic_seqdb.h"
 
 namespace {
@@ -47,7 +52,7 @@ void usage(const char *prog) {
   fprintf(stderr, "USAGE:  %s [options] <seqStorePath>\n", prog);
   fprintf(stderr, "  -partial -h a-b -H a-b -r a-b -R a-b -k <int|file> -m -u -z -t <n>\n");
   fprintf(stderr, "  --hashbits n --hashdatalen n --hashload f --maxerate f --alignnoise f\n");
-  fprintf(stderr, "  --minlength n --minkmers -o out.ovb -s out.stats [--gpu-device d] [--ovb-snappy]\n");
+  fprintf(stderr, "  --minlength n --minkmers -o out.ovb -s out.stats [--gpu-device d] [--ovb-raw]\n");
   fprintf(stderr, "  [--gpu-tune key=value,...] [--gpu-autotune nRefs]\n");
 }
 
@@ -82,58 +87,19 @@ int readSkipFile(const char *path, uint32_t K, std::string &out) {
   return 0;
 }
 
-// ---- snappy framing (literal-only blocks), the stream format ovFile::writeBuffer emits
-// ([u64 compressed length][snappy raw block] per buffer; ovStoreFile.C:212-248).  A
-// literal-only block is a valid snappy encoding: the uncompressed length as a varint,
-// then literal elements of at most 64 KiB.
-void putVarint(std::vector<uint8_t> &b, uint64_t v) {
-  while (v >= 0x80) {
-    b.push_back((uint8_t)(v | 0x80));
-    v >>= 7;
-  }
-  b.push_back((uint8_t)v);
-}
-
-void snappyLiteralBlock(const uint8_t *src, size_t n, std::vector<uint8_t> &dst) {
-  dst.clear();
-  putVarint(dst, n);
-  size_t p = 0;
-  while (p < n) {
-    size_t k = std::min<size_t>(n - p, 65536);
-    size_t l = k - 1;
-    if (l < 60) dst.push_back((uint8_t)(l << 2));
-    else if (l < 256) { dst.push_back(60 << 2); dst.push_back((uint8_t)l); }
-    else { dst.push_back(61 << 2); dst.push_back((uint8_t)(l & 0xff)); dst.push_back((uint8_t)(l >> 8)); }
-    dst.insert(dst.end(), src + p, src + p + k);
-    p += k;
-  }
-}
-
-int writeOvb(const char *path, const std::vector<uint32_t> &rec, bool snappy) {
+// Opens path for writing and closes it again: the check the reference makes when it
+// creates its output files, before any work.
+bool canWrite(const char *path) {
   FILE *F = fopen(path, "wb");
   if (!F) {
     fprintf(stderr, "Failed to open '%s' for writing: %s\n", path, strerror(errno));
-    return 1;
+    return false;
   }
-  bool bad = false;
-  if (!snappy) {
-    if (!rec.empty()) bad = fwrite(rec.data(), 4, rec.size(), F) != rec.size();
-  } else {
-    // ovFile buffer: a whole number of 6-word records, lcm of the two record sizes
-    // (ovStoreFile.C:112-121), default 1 MiB buffer.
-    const size_t lcm = (4 * 1 + 16) * (4 * 2 + 16);
-    const size_t bufWords = ((1024 * 1024) / (lcm * 4)) * lcm;
-    std::vector<uint8_t> blk;
-    for (size_t p = 0; p < rec.size(); p += bufWords) {
-      size_t   n = std::min(bufWords, rec.size() - p);
-      snappyLiteralBlock((const uint8_t *)(rec.data() + p), n * 4, blk);
-      uint64_t bl = blk.size();
-      bad |= fwrite(&bl, 8, 1, F) != 1;
-      bad |= fwrite(blk.data(), 1, blk.size(), F) != blk.size();
-    }
+  if (fclose(F) != 0) {
+    fprintf(stderr, "Failed to close '%s': %s\n", path, strerror(errno));
+    return false;
   }
-  bad |= fclose(F) != 0;
-  return bad ? 1 : 0;
+  return true;
 }
 
 // --gpu-tune key=value[,key=value...] into an oic_tuning.
@@ -171,7 +137,7 @@ int main(int argc, char **argv) {
   P.numThreads = 1;
   const char *store = nullptr, *outName = nullptr, *statName = nullptr, *skipFile = nullptr;
   int         device = 0, err = 0;
-  bool        snappy = false, haveTune = false;
+  bool        snappy = true, haveTune = false;
   oic_tuning  tune{};
   uint32_t    autotuneRefs = 0;
 
@@ -213,6 +179,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(o, "-z")) P.useHopelessCheck = 0;
     else if (!strcmp(o, "--gpu-device")) device = atoi(nxt());
     else if (!strcmp(o, "--ovb-snappy")) snappy = true;
+    else if (!strcmp(o, "--ovb-raw")) snappy = false;
     else if (!strcmp(o, "--gpu-tune")) {
       haveTune = true;
       if (!parseTuning(nxt(), tune)) fprintf(stderr, "bad --gpu-tune value\n"), err++;
@@ -229,6 +196,13 @@ int main(int argc, char **argv) {
     usage(argv[0]);
     return 1;
   }
+
+  char ocName[4096];
+  if (oic_oc_path(outName, ocName, sizeof(ocName))) {
+    fprintf(stderr, "Output name '%s' is too long\n", outName);
+    return 1;
+  }
+  if (!canWrite(outName) || !canWrite(ocName) || (statName && !canWrite(statName))) return 1;
 
   oic_seqdb db;
   if (oic_seqdb_load(store, &db)) {
@@ -282,42 +256,36 @@ int main(int argc, char **argv) {
   oic_get_stats(ctx, &st);
   oic_destroy(ctx);
 
-  if (writeOvb(outName, rec, snappy)) return 1;
-
-  // <prefix>.oc: u64 nOlaps, u32 oprMax, u32 opr[oprMax] (ovStoreFile.H:73-91).
-  std::string oc = outName;
-  if (oc.size() > 4 && oc.compare(oc.size() - 4, 4, ".ovb") == 0) oc.resize(oc.size() - 4);
-  oc += ".oc";
-  uint32_t              oprMax = db.nReads + 1;
-  std::vector<uint32_t> opr(oprMax, 0);
-  for (uint64_t i = 0; i < n; i++) {
-    opr[rec[6 * i + 0]]++;
-    opr[rec[6 * i + 1]]++;
+  if (oic_ovb_write(outName, rec.data(), n, snappy ? 1 : 0)) {
+    fprintf(stderr, "Failed to write '%s': %s\n", outName, strerror(errno));
+    return 1;
   }
-  if (FILE *C = fopen(oc.c_str(), "wb")) {
-    fwrite(&n, 8, 1, C);
-    fwrite(&oprMax, 4, 1, C);
-    fwrite(opr.data(), 4, oprMax, C);
-    fclose(C);
+  // <prefix>.oc: u64 nOlaps, u32 oprMax, u32 opr[oprMax] (ovStoreFile.H:73-91).
+  if (oic_oc_write(ocName, rec.data(), n, db.nReads)) {
+    fprintf(stderr, "Failed to write '%s': %s\n", ocName, strerror(errno));
+    return 1;
   }
 
   FILE *S = stderr;
-  if (statName) {
-    S = fopen(statName, "w");
-    if (!S) {
-      fprintf(stderr, "WARNING: failed to open '%s' for writing: %s\n", statName, strerror(errno));
-      S = stderr;
-    }
+  if (statName && !(S = fopen(statName, "w"))) {
+    fprintf(stderr, "Failed to open '%s' for writing: %s\n", statName, strerror(errno));
+    return 1;
   }
-  fprintf(S, " Kmer hits without olaps = %ld\n", (long)st.kmerHitsWithoutOlap);
-  fprintf(S, "    Kmer hits with olaps = %ld\n", (long)st.kmerHitsWithOlap);
-  fprintf(S, "  Multiple overlaps/pair = %ld\n", (long)st.multiOverlap);
-  fprintf(S, " Total overlaps produced = %ld\n", (long)st.totalOverlaps);
-  fprintf(S, "      Contained overlaps = %ld\n", (long)st.containedOverlaps);
-  fprintf(S, "       Dovetail overlaps = %ld\n", (long)st.dovetailOverlaps);
-  fprintf(S, "Rejected by short window = %ld\n", (long)st.badShortWindow);
-  fprintf(S, " Rejected by long window = %ld\n", (long)st.badLongWindow);
-  if (S != stderr) fclose(S);
+  int w = 0;
+  w |= fprintf(S, " Kmer hits without olaps = %ld\n", (long)st.kmerHitsWithoutOlap) < 0;
+  w |= fprintf(S, "    Kmer hits with olaps = %ld\n", (long)st.kmerHitsWithOlap) < 0;
+  w |= fprintf(S, "  Multiple overlaps/pair = %ld\n", (long)st.multiOverlap) < 0;
+  w |= fprintf(S, " Total overlaps produced = %ld\n", (long)st.totalOverlaps) < 0;
+  w |= fprintf(S, "      Contained overlaps = %ld\n", (long)st.containedOverlaps) < 0;
+  w |= fprintf(S, "       Dovetail overlaps = %ld\n", (long)st.dovetailOverlaps) < 0;
+  w |= fprintf(S, "Rejected by short window = %ld\n", (long)st.badShortWindow) < 0;
+  w |= fprintf(S, " Rejected by long window = %ld\n", (long)st.badLongWindow) < 0;
+  if (S != stderr) w |= fclose(S) != 0;
+  else w |= fflush(S) != 0;
+  if (w) {
+    fprintf(stderr, "Failed to write the stats to '%s': %s\n", statName ? statName : "stderr", strerror(errno));
+    return 1;
+  }
 
   fprintf(stderr, "GPU: %lu overlaps; %lu seeds, %lu pairs, %lu extensions, %lu DP cells (%lu in pairs without "
                   "overlap), %lu rows; hash %.2f ms, seed %.2f ms, align %.2f ms, total %.2f ms\n",

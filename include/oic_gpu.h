@@ -143,16 +143,19 @@ typedef struct oic_extend_problem {
 } oic_extend_problem;
 
 /* No counterpart in the reference.  oic_extend_batch() for callers that cannot call
- * cudaMalloc when they align -- code running under stream capture, programs whose
- * memory pool owns the device, plugins with a fixed memory budget.  Problems and
- * outputs are caller-owned DEVICE buffers (dOut: 5 per problem, as oic_extend_batch;
- * dStatus: 0, or the capacity flag a problem hit).  The DP's scratch is a static
- * device array of 23,072,768 bytes that every GPU loading the library holds until
- * exit; the call allocates nothing.  Limit: each problem may keep at most 131072 DP
- * cells and 8191 error rows per side of its seed match, otherwise the call returns
- * OIC_ERR_OVERFLOW.  The first call on a device looks up the array's address (make it
- * before any stream capture); calls that overlap on the GPU share the array and race.
- * Runs on the context's stream and returns when the kernel has finished. */
+ * cudaMalloc when they align: programs whose own allocator holds the whole device
+ * memory pool, and plugins given a fixed device-memory budget by their host program.
+ * Problems and outputs are caller-owned DEVICE buffers (dOut: 5 per problem, as
+ * oic_extend_batch; dStatus: 0, or the capacity/validity flag a problem hit).  The DP's
+ * scratch is a static device array of 23,072,768 bytes that every GPU loading the
+ * library holds until exit; the call allocates nothing.  Limit: each problem may keep
+ * at most 131072 DP cells and 8191 error rows per side of its seed match, otherwise its
+ * dStatus is nonzero and the call returns OIC_ERR_OVERFLOW (the other problems' outputs
+ * are still exact); a problem naming a read outside the store or a match outside its
+ * reads makes the call return OIC_ERR_ARG.  The first call on a device looks up the
+ * array's device address (make it before any stream capture; a cudaDeviceReset of that
+ * device invalidates the lookup).  Every call shares the array: calls that overlap on
+ * the GPU race.  Runs on the context's stream and returns when the kernel has finished. */
 int oic_extend_batch_noalloc(oic_ctx *ctx, uint32_t nAlign, const oic_extend_problem *dProblems, int32_t *dOut,
                              int32_t *dKind, int32_t *dDeltaLen, uint32_t *dStatus);
 
@@ -193,16 +196,27 @@ typedef struct oic_pair_info {
   uint32_t extLimit;   /* 1 when the filter's single-extension tier applied, else 0 */
 } oic_pair_info;
 
+/* The overlapInCore parameters a filter network was trained under.  A network scores
+ * seed patterns whose meaning depends on them (k-mer size, error rate, minimum overlap),
+ * so it is only used on a context with the same values. */
+typedef struct oic_filter_domain {
+  uint32_t kmerLen;      /* -k */
+  int32_t  minOlapLen;   /* --minlength */
+  double   maxErate;     /* --maxerate, strtof-rounded as in oic_params */
+} oic_filter_domain;
+
 /* Set the filter (params: host array of OIC_FILTER_NPARAM FP16 bit patterns) and its
  * probability thresholds, p = sigmoid(logit):
  *   p <  dropThreshold                  the pair is not extended;
  *   dropThreshold <= p < fullThreshold  the pair stops once extBudget extensions (0
  *                                       means 1) have run without finding an overlap;
  *   p >= fullThreshold                  every match is extended (the reference's rule).
- * fullThreshold <= dropThreshold disables the middle tier.  params NULL turns the
- * filter off. */
+ * fullThreshold <= dropThreshold disables the middle tier.  trainedOn names the
+ * parameters the network was trained under; a context whose kmerLen, minOlapLen or
+ * maxErate differs (or a NULL trainedOn) is refused with OIC_ERR_ARG.  params NULL
+ * turns the filter off. */
 int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float dropThreshold, float fullThreshold,
-                   uint32_t extBudget);
+                   uint32_t extBudget, const oic_filter_domain *trainedOn);
 
 /* Pair collection for training and evaluation: mode 0 off, 1 pairs and feature rows,
  * 2 also the match runs (T offset, length, S start per run).  Collected data accumulate

@@ -72,14 +72,17 @@ def load_golden(name):
 
 
 def run_cli(binary, args_template, db, skip, workdir, extra=()):
+    """Run the drop-in CLI (snappy-framed .ovb, as canu's ovFile writes) or the oracle's
+    CLI (the same records unframed); returns (sorted records, .oc bytes, stats, log)."""
     out = os.path.join(workdir, "out.ovb")
     stats = os.path.join(workdir, "out.stats")
     args = args_template.format(db=db, skip=skip or "").split()
     r = subprocess.run([binary] + args + list(extra) + ["-o", out, "-s", stats], stdout=subprocess.PIPE,
                        stderr=subprocess.PIPE, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    from canu_gb300 import sort_records
-    rec = sort_records(np.fromfile(out, dtype=np.uint32).reshape(-1, 6))
+    from canu_gb300 import read_ovb, sort_records
+    framed = os.path.basename(binary) == "overlapInCore"
+    rec = sort_records(read_ovb(out) if framed else np.fromfile(out, dtype=np.uint32).reshape(-1, 6))
     oc = open(os.path.join(workdir, "out.oc"), "rb").read()
     st = open(stats).read()
     return rec, oc, st, r.stderr

@@ -98,7 +98,7 @@ def load_records(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CANU_SRC") or os.path.join(ROOT, "..", "reference"))
     a = ap.parse_args()
     from canu_gb300.build import build_tools, build_lib
     build_lib()

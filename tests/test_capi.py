@@ -10,9 +10,9 @@ import canu_gb300 as oic
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    src = open(os.path.join(ROOT, "include", "oic_gpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char \*)\s*(oic_\w+)\s*\(", src, re.M)))
+def header_functions(header="oic_gpu.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|size_t|const char \*)\s*(oic_\w+)\s*\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol(built):
@@ -22,6 +22,10 @@ def test_library_exports_every_declared_symbol(built):
     for n in names:
         assert hasattr(lib, n), n
     assert set(names) == set(oic.EXPORTS)
+    files = header_functions("oic_ovfile.h")
+    for n in files:
+        assert hasattr(lib, n), n
+    assert set(files) == set(oic.OVFILE_EXPORTS)
 
 
 def test_default_params_match_reference_defaults(built):

@@ -45,7 +45,8 @@ def run_both(built, oracle, tmp, seqs, args):
         r = subprocess.run([tool] + args + ["-o", out, "-s", st, db], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
                            text=True)
         assert r.returncode == 0, (name, r.stderr[-2000:])
-        rec = oic.sort_records(np.fromfile(out, dtype=np.uint32)) if os.path.getsize(out) else np.zeros((0, 6), np.uint32)
+        raw = oic.read_ovb(out) if name == "gpu" else np.fromfile(out, dtype=np.uint32).reshape(-1, 6)
+        rec = oic.sort_records(raw)
         res.append((rec, open(out[:-4] + ".oc", "rb").read(), open(st).read()))
     (g, goc, gst), (p, poc, pst) = res
     assert g.shape == p.shape and (g == p).all()

@@ -204,7 +204,7 @@ def test_filtered_output_is_an_exact_subset(small_c2):
             ov.set_reads_seqdb(db)
             ov.set_skip_kmers(workloads.read_skip(skip))
             if params is not None:
-                ov.set_filter(params, thr)
+                ov.set_filter(params, thr, domain=filter_train.training_domain("c2"))
             if collect:
                 ov.collect_pairs(1)
             ov.run()
@@ -247,3 +247,24 @@ def test_trained_filter_gains_over_the_plain_path(small_c2):
     assert ev["recall"] >= 0.995
     assert ev["dp_cells_skipped_frac"] > 0.3
     assert ev["filter"]["dp_cells"] < ev["plain"]["dp_cells"]
+
+
+def test_filter_is_refused_outside_its_training_parameters(small_c2):
+    """The shipped network was trained at -k 22 --minlength 1000 --maxerate 0.01 on
+    0.5 %-error reads; on other parameters (here the smoke run's --maxerate 0.06
+    --minlength 500) its scores mean nothing, so the library refuses it."""
+    path = os.path.join(ROOT, "canu_gb300", "filter_c2.npz")
+    params, thr, full, meta = filter_train.load(path)
+    assert meta["domain"] == filter_train.training_domain("c2")
+    d, (db, _) = small_c2
+    for over in ({"maxErate": 0.06, "minOlapLen": 500}, {"maxErate": 0.06}, {"minOlapLen": 500}, {"kmerLen": 20}):
+        with oic.Overlapper(workloads.params("c2", **over), 0) as ov:
+            ov.set_reads_seqdb(db)
+            with pytest.raises(oic.OicError) as e:
+                ov.set_filter(params, thr, full, meta["budget"], domain=meta["domain"])
+            assert e.value.code == oic.OIC_ERR_ARG and "trained for" in str(e.value)
+            with pytest.raises(oic.OicError):
+                ov.set_filter(params, thr, full, meta["budget"])          # no domain given
+    with oic.Overlapper(workloads.params("c2"), 0) as ov:
+        ov.set_reads_seqdb(db)
+        ov.set_filter(params, thr, full, meta["budget"], domain=meta["domain"])   # its own parameters: accepted

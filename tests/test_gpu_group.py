@@ -112,7 +112,7 @@ def test_captured_graph_matches_kernel_by_kernel(built, tmp_path_factory):
             ov.set_skip_kmers(workloads.read_skip(skip))
             ov.set_tuning(noGraph=no_graph, wideArena=SMALL_ARENA, wideCtas=64)
             if filt:
-                ov.set_filter(params, thr, full, meta["budget"])
+                ov.set_filter(params, thr, full, meta["budget"], domain=meta["domain"])
             ov.run()
             return oic.sort_records(ov.overlaps()), ov.stats()
 
