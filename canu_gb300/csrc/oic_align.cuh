@@ -63,14 +63,14 @@ static __device__ __forceinline__ WarpScratch warp_scratch(const WarpScratch &ba
 
 // Row-0 exact slide shared by the warp: each lane tests one 32-base window per step.
 template <int STEP>
-__device__ __forceinline__ int warp_slide0(const SeqView &A, i64 a0, const SeqView &T, i64 t0, int m,
+__device__ __forceinline__ int warp_slide0(const SeqView &A, int a0, const SeqView &T, int t0, int m,
                                            unsigned long long &slides) {
   const int lane = threadIdx.x & 31;
   int       base = 0;
   while (base < m) {
     int off = base + lane * 32;
     int r   = 32;
-    if (off < m) r = match_run32<STEP>(A, a0 + STEP * (i64)off, T, t0 + STEP * (i64)off);
+    if (off < m) r = match_run32<STEP>(A, a0 + STEP * off, T, t0 + STEP * off);
     unsigned short_ = __ballot_sync(0xffffffffu, off < m && r < 32);
     if (short_) {
       int first = __ffs(short_) - 1;
@@ -239,7 +239,7 @@ struct RowsOut {
 // hands each extension's row loop to the whole CTA through GroupShared.
 struct GroupJob {
   SeqView A, T;
-  i64     a0, t0;
+  int     a0, t0;
   int     m, n, errorLimit, step, u;
   int    *rowA, *rowB;       // row buffers (rowA holds row 0)
 };
@@ -257,8 +257,8 @@ __device__ __forceinline__ void group_bar(int id, int nThr) {
 
 // The row loop by one warp.  Row 0 (value r0) is in prev[2].
 template <int STEP>
-__device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, i64 a0, int m, const SeqView &Tref,
-                                             i64 t0, int n, int errorLimit) {
+__device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, int a0, int m, const SeqView &Tref,
+                                             int t0, int n, int errorLimit) {
   const SeqView A = Aref, T = Tref;   // in registers for the slides
   const int lane = threadIdx.x & 31;
   RowsOut o;
@@ -378,7 +378,7 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
                                                   unsigned long long &slides) {
   const int lane = tid & 31, wid = tid >> 5, nW = nThr >> 5;
   const SeqView A = j.A, T = j.T;   // in registers for the slides
-  const i64     a0 = j.a0, t0 = j.t0;
+  const int     a0 = j.a0, t0 = j.t0;
   const int     m = j.m, n = j.n;
   RowsOut o;
   o.status = kRowsDone;
@@ -526,7 +526,7 @@ static __device__ __noinline__ void group_worker(GroupShared &gs, const WarpScra
 // set (warp 0 of a group CTA); the rest runs on this warp.  Returns the error count;
 // the outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
 template <int STEP, bool GROUP>
-static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i64 a0, int m, const SeqView &T, i64 t0, int n,
+static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, int a0, int m, const SeqView &T, int t0, int n,
                               int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
   const int lane = threadIdx.x & 31;
   const double BMV = w.P.branchMatchValue;

@@ -57,18 +57,17 @@ struct ReadsDev {
   u32 nReads;
 };
 
-// One read strand viewed as a base sequence: base i is at global base index gbase+i.
+// One read strand viewed as a base sequence: base i is base i of the read's first word.
 struct SeqView {
-  const u64 *w;
-  const u64 *nm;   // nullptr when the read has no N
-  i64        gbase;
+  const u64 *w;    // the read's first word in its strand array
+  const u64 *nm;   // its first N-mask word; nullptr when the read has no N
 };
 
 __device__ __forceinline__ SeqView make_view(const ReadsDev &R, u32 readIdx, int rev) {
   SeqView v;
-  v.w     = rev ? R.rc : R.fwd;
-  v.nm    = R.hasN[readIdx] ? (rev ? R.nrc : R.nfwd) : nullptr;
-  v.gbase = (i64)R.wordOff[readIdx] * 32;
+  const u64 wo = R.wordOff[readIdx];
+  v.w  = (rev ? R.rc : R.fwd) + wo;
+  v.nm = R.hasN[readIdx] ? (rev ? R.nrc : R.nfwd) + wo : nullptr;
   return v;
 }
 
@@ -83,28 +82,38 @@ __device__ __forceinline__ u64 load_win(const u64 *w, i64 g) {
   return (lo >> sh) | ((hi << 1) << (63 - sh));
 }
 
-// 32 bases g, g-1, ..., g-31 (base g in bits 0-1; the two bits of each base come out
-// swapped, which equality tests do not see).
-__device__ __forceinline__ u64 load_win_rev(const u64 *w, i64 g) { return __brevll(load_win(w, g - 31)); }
+// The same for base g of one read (w = the read's first word; -32 < g: the guard word
+// before every read keeps g - 31 in bounds), in 32-bit index arithmetic.
+__device__ __forceinline__ u64 load_win32(const u64 *w, int g) {
+  const int wi = g >> 5;
+  const int sh = (g & 31) * 2;
+  const u64 lo = __ldg(w + wi);
+  const u64 hi = __ldg(w + wi + 1);
+  return (lo >> sh) | ((hi << 1) << (63 - sh));
+}
+
+// 32 bases g, g-1, ..., g-31 of one read (base g in bits 0-1; the two bits of each
+// base come out swapped, which equality tests do not see).
+__device__ __forceinline__ u64 load_win_rev(const u64 *w, int g) { return __brevll(load_win32(w, g - 31)); }
 
 // Number of leading bases (0..32) that agree between A (from a) and T (from t), with
 // N matching anything (prefixEditDistance-forward.C:164 / -reverse.C:186).
 template <int STEP>
-__device__ __forceinline__ int match_run32(const SeqView &A, i64 a, const SeqView &T, i64 t) {
+__device__ __forceinline__ int match_run32(const SeqView &A, int a, const SeqView &T, int t) {
   u64 wa, wt;
   if (STEP > 0) {
-    wa = load_win(A.w, A.gbase + a);
-    wt = load_win(T.w, T.gbase + t);
+    wa = load_win32(A.w, a);
+    wt = load_win32(T.w, t);
   } else {
-    wa = load_win_rev(A.w, A.gbase + a);
-    wt = load_win_rev(T.w, T.gbase + t);
+    wa = load_win_rev(A.w, a);
+    wt = load_win_rev(T.w, t);
   }
   u64 x  = wa ^ wt;
   u64 mm = (x | (x >> 1)) & kPairMask;
   if (mm && (A.nm || T.nm)) {
     u64 n = 0;
-    if (A.nm) n |= (STEP > 0) ? load_win(A.nm, A.gbase + a) : load_win_rev(A.nm, A.gbase + a);
-    if (T.nm) n |= (STEP > 0) ? load_win(T.nm, T.gbase + t) : load_win_rev(T.nm, T.gbase + t);
+    if (A.nm) n |= (STEP > 0) ? load_win32(A.nm, a) : load_win_rev(A.nm, a);
+    if (T.nm) n |= (STEP > 0) ? load_win32(T.nm, t) : load_win_rev(T.nm, t);
     mm &= ~n;
   }
   return mm ? (__ffsll((long long)mm) - 1) >> 1 : 32;
@@ -112,11 +121,11 @@ __device__ __forceinline__ int match_run32(const SeqView &A, i64 a, const SeqVie
 
 // Bases that agree from A[step*row] / T[step*(row+d)] on, capped at `lim`.
 template <int STEP>
-__device__ __forceinline__ int slide(const SeqView &A, i64 a0, const SeqView &T, i64 t0, int row, int d, int lim,
+__device__ __forceinline__ int slide(const SeqView &A, int a0, const SeqView &T, int t0, int row, int d, int lim,
                                      unsigned long long &slides) {
   int run = 0;
   while (run < lim) {
-    int r = match_run32<STEP>(A, a0 + STEP * (i64)(row + run), T, t0 + STEP * (i64)(row + d + run));
+    int r = match_run32<STEP>(A, a0 + STEP * (row + run), T, t0 + STEP * (row + d + run));
     run += r;
     if (r < 32) break;
   }

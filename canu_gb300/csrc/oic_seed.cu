@@ -128,8 +128,8 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
       const int i = i0 + lane;
       u32 n = 0, qEnd = 0;
       if (i < nK) {
-        u64 key = load_win(S.w, S.gbase + i) & kmask;
-        bool ok = !(S.nm && (load_win(S.nm, S.gbase + i) & kmask));
+        u64 key = load_win32(S.w, i) & kmask;
+        bool ok = !(S.nm && (load_win32(S.nm, i) & kmask));
         u64 val;
         if (ok && table_find(T, key, val)) {
           if (val >> 63) {
