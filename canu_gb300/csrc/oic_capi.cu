@@ -131,8 +131,9 @@ struct oic_ctx {
   bool     haveBlock = false;
   uint32_t blkFirst = 0, blkN = 0;
   uint64_t blkOcc = 0, blkDistinct = 0;
-  DevBuf dTKeys, dTVals, dOcc, dLscr, dRscr, dSlen, dSread;
+  DevBuf dTable, dOcc, dLscr, dRscr, dSlen, dSread;   // dTable: 16-byte (key, value) slots
   DevBuf dSortK, dSortV, dSortK2, dSortV2, dFlags, dPos, dSortScratch, dStrRead, dStrKmers, dFlat, dNewKeys;
+  DevBuf dChunkStr;   // block string of every 4096th flat k-mer index
   TableDev T{};
 
   // seeds
@@ -230,9 +231,11 @@ struct SeedConfig {
   SeedCaps caps;
 };
 
+// Seed configurations, tried in this order for a ref strand: pair table and node
+// pool in HBM scratch on four warps per SM slot; in large HBM scratch on one warp per SM.
 SeedConfig seed_normal(const oic_ctx *c) {
   SeedConfig s;
-  s.warps        = c->nSM * 8 * 4;
+  s.warps           = c->nSM * 8 * 4;
   s.caps.slotCap = 4096;
   s.caps.pairCap = 2048;
   s.caps.nodeCap = 32768;
@@ -437,45 +440,38 @@ int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t e
   so.err           = ctr32(ctx) + cErr;
 
   CK(cudaEventRecord(evSeed0, ctx->st));
-  SeedConfig sn = seed_normal(ctx);
-  SeedScratch ss;
-  int rc = ensure_seed_scratch(ctx, sn, false, ss);
-  if (rc) return rc;
-  launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), nullptr, nSeg, ctr32(ctx) + cSegCounter, ss,
-              sn.caps, sn.warps, so, ctx->st);
+  // Strands whose pair table or node pool overflowed run again in the wide
+  // configuration, their ids being the work list of that pass.
+  const SeedConfig tiers[2] = {seed_normal(ctx), seed_wide(ctx)};
   uint32_t h[16];
-  CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-  if ((rc = sync_check(ctx, "seed kernel"))) return rc;
-  if (h[cErr] & (kErrOutNodes | kErrOutPairs)) {
-    // Every segment reserved its output with one atomic add, so the counters hold the
-    // batch's whole demand.
-    ctx->overPairs = h[cPairCount];
-    ctx->overNodes = h[cNodeCount];
-    return kRetrySmaller;
-  }
-  if (h[cSegOvf] > 0) {
-    // Segments whose pair table or node pool overflowed run again in the wide
-    // configuration; their ids are the work list of that pass.
-    const uint32_t nOvf = h[cSegOvf];
-    if (verbose()) fprintf(stderr, "oic: %u ref strands rerun in the wide seed configuration\n", nOvf);
-    CK(ctx->dSegList.ensure((size_t)nOvf * sizeof(uint32_t)));
-    CK(cudaMemcpyAsync(ctx->dSegList.p, ctx->dSegOvf.p, nOvf * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->st));
-    CK(cudaMemsetAsync(ctr32(ctx) + cSegCounter, 0, sizeof(uint32_t), ctx->st));
-    CK(cudaMemsetAsync(ctr32(ctx) + cSegOvf, 0, sizeof(uint32_t), ctx->st));
-    SeedConfig sw = seed_wide(ctx);
-    SeedScratch ssw;
-    if ((rc = ensure_seed_scratch(ctx, sw, true, ssw))) return rc;
-    launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), ctx->dSegList.as<uint32_t>(), nOvf,
-                ctr32(ctx) + cSegCounter, ssw, sw.caps, sw.warps, so, ctx->st);
+  int      rc    = OIC_OK;
+  uint32_t nTodo = nSeg;
+  for (int t = 0; t < 2; t++) {
+    SeedScratch ss;
+    if ((rc = ensure_seed_scratch(ctx, tiers[t], t == 1, ss))) return rc;
+    if (t > 0) {
+      if (verbose()) fprintf(stderr, "oic: %u ref strands rerun in seed configuration %d\n", nTodo, t);
+      CK(ctx->dSegList.ensure((size_t)nTodo * sizeof(uint32_t)));
+      CK(cudaMemcpyAsync(ctx->dSegList.p, ctx->dSegOvf.p, nTodo * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                         ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cSegCounter, 0, sizeof(uint32_t), ctx->st));
+      CK(cudaMemsetAsync(ctr32(ctx) + cSegOvf, 0, sizeof(uint32_t), ctx->st));
+    }
+    launch_seed(ctx->R, ctx->T, ctx->dp, ctx->dSegReads.as<uint32_t>(), t ? ctx->dSegList.as<uint32_t>() : nullptr,
+                nTodo, ctr32(ctx) + cSegCounter, ss, tiers[t].caps, tiers[t].warps, so, ctx->st);
     CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
-    if ((rc = sync_check(ctx, "seed kernel (wide)"))) return rc;
+    if ((rc = sync_check(ctx, "seed kernel"))) return rc;
     if (h[cErr] & (kErrOutNodes | kErrOutPairs)) {
+      // Every segment reserved its output with one atomic add, so the counters hold the
+      // batch's whole demand.
       ctx->overPairs = h[cPairCount];
       ctx->overNodes = h[cNodeCount];
       return kRetrySmaller;
     }
-    if (h[cSegOvf] > 0)
+    if (h[cSegOvf] == 0) break;
+    if (t == 1)
       return fail(ctx, OIC_ERR_OVERFLOW, "a ref read has more candidate pairs or match nodes than the engine holds");
+    nTodo = h[cSegOvf];
   }
   CK(cudaEventRecord(evSeed1, ctx->st));
   nPairs = h[cPairCount];
@@ -1128,10 +1124,10 @@ void oic_destroy(oic_ctx *ctx) {
   cudaSetDevice(ctx->device);
   DevBuf *bufs[] = {&ctx->dEml,      &ctx->dFwd,        &ctx->dRc,         &ctx->dNfwd,      &ctx->dNrc,
                     &ctx->dWordOff,  &ctx->dLen,        &ctx->dLib,        &ctx->dHasN,      &ctx->dSkip,
-                    &ctx->dTKeys,    &ctx->dTVals,      &ctx->dOcc,        &ctx->dLscr,      &ctx->dRscr,
+                    &ctx->dTable,     &ctx->dOcc,        &ctx->dLscr,      &ctx->dRscr,
                     &ctx->dSlen,     &ctx->dSread,      &ctx->dSortK,      &ctx->dSortV,     &ctx->dSortK2,
                     &ctx->dSortV2,   &ctx->dFlags,      &ctx->dPos,        &ctx->dSortScratch, &ctx->dStrRead,
-                    &ctx->dStrKmers, &ctx->dFlat,       &ctx->dNewKeys,    &ctx->dSegReads,  &ctx->dPairs,
+                    &ctx->dStrKmers, &ctx->dFlat,       &ctx->dNewKeys,    &ctx->dChunkStr,    &ctx->dSegReads,  &ctx->dPairs,
                     &ctx->dNodes,    &ctx->dSegOvf,     &ctx->dSeedSlotK,  &ctx->dSeedSlotV, &ctx->dSeedPairs,
                     &ctx->dSeedNodes, &ctx->dSeedSlotK2, &ctx->dSeedSlotV2, &ctx->dSeedPairs2, &ctx->dSeedNodes2,
                     &ctx->dWork,     &ctx->dRec,        &ctx->dCnt,        &ctx->dRecPos,    &ctx->dRecOut,
@@ -1179,7 +1175,7 @@ int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const ui
     w += (length[i] + 31) / 32 + 1;
   }
   ctx->wordOff[nReads] = w;
-  const uint64_t nWords = w + 2;
+  const uint64_t nWords = w + 4;   // spare words: 32-base windows and staged tiles past the last read
 
   cudaEvent_t r0, r1;
   cudaEventCreate(&r0);
@@ -1301,10 +1297,12 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
   CK(ctx->dStrKmers.ensure((size_t)nCand * 4 + 4));
   CK(ctx->dFlat.ensure((size_t)(nCand + 1) * 8));
   CK(ctx->dNewKeys.ensure((size_t)nCand * 4 + 4));
+  CK(ctx->dChunkStr.ensure(((size_t)(nFlat >> 12) + 1) * 4));
   CK(cudaMemcpyAsync(ctx->dStrRead.p, strRead.data(), nCand * 4, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemcpyAsync(ctx->dStrKmers.p, strKmers.data(), nCand * 4, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemcpyAsync(ctx->dFlat.p, flat.data(), (size_t)(nCand + 1) * 8, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemsetAsync(ctx->dNewKeys.p, 0, (size_t)nCand * 4 + 4, ctx->st));
+  if (nCand) launch_chunk_str(ctx->dFlat.as<u64>(), nCand, nFlat, ctx->dChunkStr.as<uint32_t>(), ctx->st);
 
   const size_t n = (size_t)nFlat;
   CK(ctx->dSortK.ensure(n * 8 + 8));
@@ -1319,7 +1317,8 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
                    (int)K, ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), ctx->st);
   CK(radix_sort_u64_u32(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), ctx->dSortK2.as<u64>(),
                         ctx->dSortV2.as<uint32_t>(), n, 2 * (int)K + 1, ctx->dSortScratch.p, ctx->st));
-  launch_first_occ(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), n, ctx->dFlat.as<u64>(), nCand, (int)K,
+  launch_first_occ(ctx->dSortK.as<u64>(), ctx->dSortV.as<uint32_t>(), n, ctx->dFlat.as<u64>(),
+                   ctx->dChunkStr.as<uint32_t>(), (int)K,
                    ctx->dNewKeys.as<uint32_t>(), ctx->st);
   std::vector<uint32_t> newKeys(nCand);
   CK(cudaMemcpyAsync(newKeys.data(), ctx->dNewKeys.p, (size_t)nCand * 4, cudaMemcpyDeviceToHost, ctx->st));
@@ -1350,15 +1349,13 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
 
   uint64_t cap = 1024;
   while (cap < 2 * (distinct + ctx->skipKeys.size() + 1)) cap <<= 1;
-  CK(ctx->dTKeys.ensure(cap * 8));
-  CK(ctx->dTVals.ensure(cap * 8));
+  // Slots of 16 bytes: empty key (all ones), value 0.
+  CK(ctx->dTable.ensure(cap * 16));
   CK(ctx->dOcc.ensure((size_t)nOcc * 8 + 8));
-  CK(cudaMemsetAsync(ctx->dTKeys.p, 0xff, cap * 8, ctx->st));
-  CK(cudaMemsetAsync(ctx->dTVals.p, 0, cap * 8, ctx->st));
+  launch_table_init(ctx->dTable.as<u64>(), cap, ctx->st);
   CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, 4, ctx->st));
-  launch_table_build(ctx->dSortK2.as<u64>(), nOcc, ctx->dTKeys.as<u64>(), ctx->dTVals.as<u64>(), cap - 1,
-                     ctr32(ctx) + cErr, ctx->st);
-  launch_occ_convert(ctx->dSortV2.as<uint32_t>(), nOcc, ctx->dFlat.as<u64>(), std::max<uint32_t>(nStr, 1),
+  launch_table_build(ctx->dSortK2.as<u64>(), nOcc, ctx->dTable.as<u64>(), cap - 1, ctr32(ctx) + cErr, ctx->st);
+  launch_occ_convert(ctx->dSortV2.as<uint32_t>(), nOcc, ctx->dFlat.as<u64>(), ctx->dChunkStr.as<uint32_t>(),
                      ctx->dOcc.as<u64>(), ctx->st);
 
   // String_Info (Build_Hash_Index.C:511-536): loaded strings unscreened, skipped ones screened.
@@ -1379,8 +1376,7 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
   CK(cudaMemcpyAsync(ctx->dSread.p, sread.data(), (size_t)nStr * 4, cudaMemcpyHostToDevice, ctx->st));
 
   TableDev &T = ctx->T;
-  T.keys     = ctx->dTKeys.as<u64>();
-  T.vals     = ctx->dTVals.as<u64>();
+  T.kv       = ctx->dTable.as<u64>();
   T.mask     = cap - 1;
   T.occ      = ctx->dOcc.as<u64>();
   T.lscr     = ctx->dLscr.as<unsigned char>();
@@ -1393,7 +1389,7 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
   if (!ctx->skipKeys.empty()) {
     CK(ctx->dSkip.ensure(ctx->skipKeys.size() * 8));
     CK(cudaMemcpyAsync(ctx->dSkip.p, ctx->skipKeys.data(), ctx->skipKeys.size() * 8, cudaMemcpyHostToDevice, ctx->st));
-    launch_skip_mark(ctx->dSkip.as<u64>(), ctx->skipKeys.size(), T, ctx->dTKeys.as<u64>(), ctx->dTVals.as<u64>(),
+    launch_skip_mark(ctx->dSkip.as<u64>(), ctx->skipKeys.size(), T, ctx->dTable.as<u64>(),
                      ctx->dLscr.as<unsigned char>(), ctx->dRscr.as<unsigned char>(), (int)K, P.useHopelessCheck ? 1 : 0,
                      ctr32(ctx) + cErr, ctx->st);
   }

@@ -143,10 +143,11 @@ __device__ __forceinline__ u64 mix64(u64 x) {
   return x;
 }
 
-// K-mer table (device).  vals: bits 0-31 first occurrence, 32-62 count, 63 screened.
+// K-mer table (device): open addressing over 16-byte slots, slot s = (key kv[2s],
+// value kv[2s+1]) so that a probe is one 16-byte load.  value: bits 0-31 first
+// occurrence, 32-62 count, 63 screened.
 struct TableDev {
-  const u64 *keys;
-  const u64 *vals;
+  const u64 *kv;
   u64        mask;       // capacity - 1
   const u64 *occ;        // (blockString << 32) | offset, ascending within a k-mer
   const unsigned char *lscr, *rscr;   // String_Info l/rfrag_end_screened per block string
@@ -159,12 +160,12 @@ struct TableDev {
 __device__ __forceinline__ bool table_find(const TableDev &T, u64 key, u64 &val) {
   u64 s = mix64(key) & T.mask;
   for (u64 probe = 0; probe <= T.mask; probe++) {
-    u64 k = __ldg(T.keys + s);
-    if (k == key) {
-      val = __ldg(T.vals + s);
+    const ulonglong2 e = __ldg((const ulonglong2 *)T.kv + s);
+    if (e.x == key) {
+      val = e.y;
       return true;
     }
-    if (k == kEmptyKey) return false;
+    if (e.x == kEmptyKey) return false;
     s = (s + 1) & T.mask;
   }
   return false;

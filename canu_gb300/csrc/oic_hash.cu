@@ -84,7 +84,17 @@ __global__ void kmer_emit_kernel(ReadsDev R, const u32 *strRead, const u32 *strK
   }
 }
 
-__device__ __forceinline__ u32 string_of(const u64 *flatStart, u32 nStr, u64 flat) {
+// Block string holding flat k-mer index `flat` (< flatStart[nStr]): the last s with
+// flatStart[s] <= flat.  chunkStr[c] is that string for flat index c << kChunkBits, so
+// the walk from it passes at most the strings that start inside one chunk.
+constexpr int kChunkBits = 12;
+__device__ __forceinline__ u32 string_of(const u64 *flatStart, const u32 *chunkStr, u64 flat) {
+  u32 s = __ldg(chunkStr + (flat >> kChunkBits));
+  while (__ldg(flatStart + s + 1) <= flat) s++;
+  return s;
+}
+
+__device__ __forceinline__ u32 string_of_search(const u64 *flatStart, u32 nStr, u64 flat) {
   // last s with flatStart[s] <= flat
   u32 lo = 0, hi = nStr;
   while (hi - lo > 1) {
@@ -95,13 +105,13 @@ __device__ __forceinline__ u32 string_of(const u64 *flatStart, u32 nStr, u64 fla
   return lo;
 }
 
-__global__ void first_occ_kernel(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, int K,
-                                 u32 *newKeys) {
+__global__ void first_occ_kernel(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr,
+                                 int K, u32 *newKeys) {
   const u64 invalid = 1ull << (2 * K);
   for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (u64)gridDim.x * blockDim.x) {
     u64 k = keys[p];
     if (k >= invalid) continue;
-    if (p == 0 || keys[p - 1] != k) atomicAdd(&newKeys[string_of(flatStart, nStr, vals[p])], 1u);
+    if (p == 0 || keys[p - 1] != k) atomicAdd(&newKeys[string_of(flatStart, chunkStr, vals[p])], 1u);
   }
 }
 
@@ -120,10 +130,10 @@ __global__ void compact_kv_kernel(const u64 *keys, const u32 *vals, const u32 *f
     }
 }
 
-__device__ __forceinline__ bool table_slot(const u64 *tKeys, u64 mask, u64 key, u64 &slot) {
+__device__ __forceinline__ bool table_slot(const u64 *tKV, u64 mask, u64 key, u64 &slot) {
   u64 s = mix64(key) & mask;
   for (u64 probe = 0; probe <= mask; probe++) {
-    u64 k = tKeys[s];
+    u64 k = tKV[2 * s];
     if (k == key) { slot = s; return true; }
     if (k == kEmptyKey) return false;
     s = (s + 1) & mask;
@@ -131,17 +141,23 @@ __device__ __forceinline__ bool table_slot(const u64 *tKeys, u64 mask, u64 key, 
   return false;
 }
 
+// Every slot empty: key all ones, value 0 (one 16-byte store per slot).
+__global__ void table_init_kernel(u64 *tKV, u64 cap) {
+  for (u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x; s < cap; s += (u64)gridDim.x * blockDim.x)
+    ((ulonglong2 *)tKV)[s] = make_ulonglong2(kEmptyKey, 0ull);
+}
+
 // Run starts claim a slot; the occurrence run begins at p.
-__global__ void table_starts_kernel(const u64 *keys, u64 n, u64 *tKeys, u64 *tVals, u64 mask, u32 *err) {
+__global__ void table_starts_kernel(const u64 *keys, u64 n, u64 *tKV, u64 mask, u32 *err) {
   for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (u64)gridDim.x * blockDim.x) {
     u64 k = keys[p];
     if (p > 0 && keys[p - 1] == k) continue;
     u64  s    = mix64(k) & mask;
     bool done = false;
     for (u64 probe = 0; probe <= mask; probe++) {
-      u64 old = atomicCAS(&tKeys[s], kEmptyKey, k);
+      u64 old = atomicCAS(&tKV[2 * s], kEmptyKey, k);
       if (old == kEmptyKey || old == k) {
-        tVals[s] = p;
+        tKV[2 * s + 1] = p;
         done     = true;
         break;
       }
@@ -152,22 +168,22 @@ __global__ void table_starts_kernel(const u64 *keys, u64 n, u64 *tKeys, u64 *tVa
 }
 
 // Run ends fill in the count.
-__global__ void table_counts_kernel(const u64 *keys, u64 n, const u64 *tKeys, u64 *tVals, u64 mask) {
+__global__ void table_counts_kernel(const u64 *keys, u64 n, u64 *tKV, u64 mask) {
   for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (u64)gridDim.x * blockDim.x) {
     u64 k = keys[p];
     if (p + 1 < n && keys[p + 1] == k) continue;
     u64 s;
-    if (table_slot(tKeys, mask, k, s)) {
-      u64 start = tVals[s] & 0xffffffffull;
-      tVals[s]  = start | ((p + 1 - start) << 32);
+    if (table_slot(tKV, mask, k, s)) {
+      u64 start      = tKV[2 * s + 1] & 0xffffffffull;
+      tKV[2 * s + 1] = start | ((p + 1 - start) << 32);
     }
   }
 }
 
-__global__ void occ_convert_kernel(const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, u64 *occ) {
+__global__ void occ_convert_kernel(const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr, u64 *occ) {
   for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (u64)gridDim.x * blockDim.x) {
     u64 flat = vals[p];
-    u32 s    = string_of(flatStart, nStr, flat);
+    u32 s    = string_of(flatStart, chunkStr, flat);
     occ[p]   = ((u64)s << 32) | (u64)(flat - flatStart[s]);
   }
 }
@@ -176,25 +192,25 @@ __global__ void occ_convert_kernel(const u32 *vals, u64 n, const u64 *flatStart,
 // screen the read ends near its occurrences (Mark_Screened_Ends_Chain, :96-121); with
 // the hopeless check on, an absent k-mer gets an empty entry of its own
 // (Add_Extra_Hash_String, :26-86) so that probes still see it as screened.
-__global__ void skip_mark_kernel(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeys, u64 *tVals,
+__global__ void skip_mark_kernel(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKV,
                                  unsigned char *lscr, unsigned char *rscr, int K, int hopeless, u32 *err) {
   for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < nSkip; i += (u64)gridDim.x * blockDim.x) {
     const u64 key = skipKeys[i];
     u64       s   = mix64(key) & T.mask;
     bool      done = false;
     for (u64 probe = 0; probe <= T.mask && !done; probe++) {
-      u64 k = tKeys[s];
+      u64 k = tKV[2 * s];
       if (k == kEmptyKey) {
         if (!hopeless) { done = true; break; }
-        k = atomicCAS(&tKeys[s], kEmptyKey, key);
+        k = atomicCAS(&tKV[2 * s], kEmptyKey, key);
         if (k == kEmptyKey) {
-          atomicOr(&tVals[s], 1ull << 63);   // count 0, screened
+          atomicOr(&tKV[2 * s + 1], 1ull << 63);   // count 0, screened
           done = true;
           break;
         }
       }
       if (k == key) {
-        u64 v = atomicOr(&tVals[s], 1ull << 63);
+        u64 v = atomicOr(&tKV[2 * s + 1], 1ull << 63);
         u32 start = (u32)(v & 0xffffffffull);
         u32 cnt   = (u32)((v >> 32) & 0x7fffffffull);
         for (u32 j = 0; j < cnt; j++) {
@@ -238,10 +254,23 @@ void launch_kmer_emit(ReadsDev R, const u32 *strRead, const u32 *strKmers, const
   g_launches++;
 }
 
-void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, int K, u32 *newKeys,
+// chunkStr[c] = block string holding flat k-mer index c << 12 (see string_of).
+__global__ void chunk_str_kernel(const u64 *flatStart, u32 nStr, u64 nChunks, u32 *chunkStr) {
+  for (u64 c = (u64)blockIdx.x * blockDim.x + threadIdx.x; c < nChunks; c += (u64)gridDim.x * blockDim.x)
+    chunkStr[c] = string_of_search(flatStart, nStr, c << kChunkBits);
+}
+
+void launch_chunk_str(const u64 *flatStart, u32 nStr, u64 nFlat, u32 *chunkStr, cudaStream_t st) {
+  const u64 nChunks = (nFlat >> kChunkBits) + 1;
+  chunk_str_kernel<<<grid_for(nChunks, 256), 256, 0, st>>>(flatStart, nStr, nChunks, chunkStr);
+  g_launches++;
+}
+
+void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr, int K,
+                      u32 *newKeys,
                       cudaStream_t st) {
   if (n == 0) return;
-  first_occ_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, vals, n, flatStart, nStr, K, newKeys);
+  first_occ_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, vals, n, flatStart, chunkStr, K, newKeys);
   g_launches++;
 }
 
@@ -258,25 +287,29 @@ void launch_compact_kv(const u64 *keys, const u32 *vals, const u32 *flags, const
   g_launches++;
 }
 
-void launch_table_build(const u64 *keys, u64 n, u64 *tKeys, u64 *tVals, u64 mask, u32 *err, cudaStream_t st) {
-  if (n == 0) return;
-  table_starts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKeys, tVals, mask, err);
-  g_launches++;
-  table_counts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKeys, tVals, mask);
+void launch_table_init(u64 *tKV, u64 cap, cudaStream_t st) {
+  table_init_kernel<<<grid_for(cap, 256), 256, 0, st>>>(tKV, cap);
   g_launches++;
 }
 
-void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, u64 *occ, cudaStream_t st) {
+void launch_table_build(const u64 *keys, u64 n, u64 *tKV, u64 mask, u32 *err, cudaStream_t st) {
   if (n == 0) return;
-  occ_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(vals, n, flatStart, nStr, occ);
+  table_starts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKV, mask, err);
+  g_launches++;
+  table_counts_kernel<<<grid_for(n, 256), 256, 0, st>>>(keys, n, tKV, mask);
   g_launches++;
 }
 
-void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeysMut, u64 *tValsMut, unsigned char *lscr,
+void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr, u64 *occ, cudaStream_t st) {
+  if (n == 0) return;
+  occ_convert_kernel<<<grid_for(n, 256), 256, 0, st>>>(vals, n, flatStart, chunkStr, occ);
+  g_launches++;
+}
+
+void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKVMut, unsigned char *lscr,
                       unsigned char *rscr, int K, int hopeless, u32 *err, cudaStream_t st) {
   if (nSkip == 0) return;
-  skip_mark_kernel<<<grid_for(nSkip, 128), 128, 0, st>>>(skipKeys, nSkip, T, tKeysMut, tValsMut, lscr, rscr, K,
-                                                         hopeless, err);
+  skip_mark_kernel<<<grid_for(nSkip, 128), 128, 0, st>>>(skipKeys, nSkip, T, tKVMut, lscr, rscr, K, hopeless, err);
   g_launches++;
 }
 

@@ -26,16 +26,22 @@ void launch_pack_reads(const char *ascii, const u64 *srcOff, const u32 *len, con
 void launch_kmer_emit(ReadsDev R, const u32 *strRead, const u32 *strKmers, const u64 *flatStart, u32 nStr, int K,
                       u64 *keys, u32 *vals, cudaStream_t st);
 // newKeys[s] += number of distinct k-mers whose first occurrence is in block string s.
-void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, int K, u32 *newKeys,
-                      cudaStream_t st);
+// chunkStr[c] (nFlat / 4096 + 1 entries) = the block string holding flat k-mer index
+// c * 4096; string lookups of the two kernels below start there.
+void launch_chunk_str(const u64 *flatStart, u32 nStr, u64 nFlat, u32 *chunkStr, cudaStream_t st);
+void launch_first_occ(const u64 *keys, const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr, int K,
+                      u32 *newKeys, cudaStream_t st);
 // flags[p] = 1 when keys[p] is a valid k-mer and vals[p] < flatLimit.
 void launch_keep_flags(const u64 *keys, const u32 *vals, u64 n, int K, u32 flatLimit, u32 *flags, cudaStream_t st);
 void launch_compact_kv(const u64 *keys, const u32 *vals, const u32 *flags, const u32 *pos, u64 n, u64 *keysOut,
                        u32 *valsOut, cudaStream_t st);
-void launch_table_build(const u64 *keys, u64 n, u64 *tKeys, u64 *tVals, u64 mask, u32 *err, cudaStream_t st);
-void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, u32 nStr, u64 *occ, cudaStream_t st);
-void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKeysMut, u64 *tValsMut,
-                      unsigned char *lscr, unsigned char *rscr, int K, int hopeless, u32 *err, cudaStream_t st);
+// Open-addressing table of 16-byte slots (key, value) at tKV, capacity mask + 1;
+// launch_table_init empties every slot.
+void launch_table_init(u64 *tKV, u64 cap, cudaStream_t st);
+void launch_table_build(const u64 *keys, u64 n, u64 *tKV, u64 mask, u32 *err, cudaStream_t st);
+void launch_occ_convert(const u32 *vals, u64 n, const u64 *flatStart, const u32 *chunkStr, u64 *occ, cudaStream_t st);
+void launch_skip_mark(const u64 *skipKeys, u64 nSkip, TableDev T, u64 *tKVMut, unsigned char *lscr,
+                      unsigned char *rscr, int K, int hopeless, u32 *err, cudaStream_t st);
 
 // ---------------- seeds ----------------
 struct PairRec {

@@ -3,7 +3,8 @@
 // Scan: three-phase (per-tile reduce, recursive scan of tile sums, per-tile scan).
 // Sort: 8-bit digits; per pass an upsweep histogram per 4096-key tile (digit-major,
 // so one exclusive scan gives every (digit, tile) its output base), then a downsweep
-// that ranks keys stably inside the tile with warp match_any and scatters them.
+// that ranks keys stably inside the tile with warp match_any, groups the tile by digit
+// in shared memory and writes each digit's run out with coalesced stores.
 #include "oic_prims.cuh"
 
 namespace oic {
@@ -150,13 +151,21 @@ __global__ void __launch_bounds__(kSortThreads) radix_upsweep_kernel(const unsig
   }
 }
 
+// Downsweep of one 4096-key tile: rank every key inside the tile (stable: warp order,
+// then item order, then lane order) with warp match_any, place the tile in shared
+// memory grouped by digit, then write each digit's run to its output range -- the
+// writes of consecutive threads go to consecutive addresses.
 __global__ void __launch_bounds__(kSortThreads) radix_downsweep_kernel(const unsigned long long *keysIn, const uint32_t *valsIn,
                                                                        unsigned long long *keysOut, uint32_t *valsOut, uint64_t n,
                                                                        int shift, const uint32_t *offsets,
                                                                        uint32_t nTiles, const uint32_t *nDev) {
+  extern __shared__ __align__(16) unsigned char sortDyn[];
+  unsigned long long *sk = (unsigned long long *)sortDyn;           // kSortTile keys
+  uint32_t           *sv = (uint32_t *)(sk + kSortTile);             // kSortTile values
   __shared__ uint32_t cnt[kSortWarps][kDigits];
+  __shared__ uint32_t tileBase[kDigits];     // output position of the tile's first key of each digit
+  __shared__ uint32_t localStart[kDigits];   // position of that key inside the tile
   if (nDev && *nDev < n) n = *nDev;
-  __shared__ uint32_t tileBase[kDigits];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * kDigits; i += kSortThreads) (&cnt[0][0])[i] = 0;
   for (int d = threadIdx.x; d < kDigits; d += kSortThreads) tileBase[d] = offsets[(uint64_t)d * nTiles + blockIdx.x];
@@ -174,6 +183,10 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep_kernel(const uns
     bool     ok = i < n;
     k[it]       = ok ? keysIn[i] : 0;
     v[it]       = ok ? valsIn[i] : 0;
+  }
+#pragma unroll
+  for (int it = 0; it < kSortItems; it++) {
+    const bool ok = base + (uint64_t)it * 32 + lane < n;
     int d       = ok ? (int)((k[it] >> shift) & 0xff) : kDigits;
     dig[it]     = d;
     unsigned peers  = __match_any_sync(0xffffffffu, d);
@@ -187,26 +200,45 @@ __global__ void __launch_bounds__(kSortThreads) radix_downsweep_kernel(const uns
     __syncwarp();
   }
   __syncthreads();
-  // Exclusive prefix of the per-warp counts, per digit.
-  for (int d = threadIdx.x; d < kDigits; d += kSortThreads) {
-    uint32_t s = tileBase[d];
+  // Per digit: the warps' exclusive prefix, then the digit's start inside the tile.
+  uint32_t tot = 0;
+  {
+    const int d = threadIdx.x;   // kSortThreads == kDigits
+    uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; w++) {
       uint32_t c = cnt[w][d];
       cnt[w][d]  = s;
       s += c;
     }
+    uint32_t all;
+    const uint32_t start = block_excl_scan(s, all);
+    localStart[d] = start;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) cnt[w][d] += start;
+    tot = all;
   }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < kSortItems; it++) {
     if (dig[it] < kDigits) {
-      uint64_t pos = (uint64_t)cnt[wid][dig[it]] + rank[it];
-      keysOut[pos] = k[it];
-      valsOut[pos] = v[it];
+      const uint32_t p = cnt[wid][dig[it]] + rank[it];
+      sk[p] = k[it];
+      sv[p] = v[it];
     }
   }
+  __syncthreads();
+  for (uint32_t p = threadIdx.x; p < tot; p += kSortThreads) {
+    const unsigned long long key = sk[p];
+    const int d = (int)((key >> shift) & 0xff);
+    const uint64_t pos = (uint64_t)tileBase[d] + (p - localStart[d]);
+    keysOut[pos] = key;
+    valsOut[pos] = sv[p];
+  }
 }
+
+constexpr size_t kDownsweepDyn = (size_t)kSortTile * (sizeof(unsigned long long) + sizeof(uint32_t));
+static_assert(kSortThreads == kDigits && kSortThreads == kScanThreads, "one digit per thread in the downsweep");
 
 }  // namespace
 
@@ -227,13 +259,20 @@ cudaError_t radix_sort_u64_u32(unsigned long long *keys, uint32_t *vals, unsigne
   unsigned long long *ks = keys, *kd = keysAlt;
   uint32_t *vs = vals, *vd = valsAlt;
   int       passes = 0;
+  static bool attrSet = false;   // opt in to the downsweep's 48 KB of dynamic shared memory (per process)
+  if (!attrSet) {
+    cudaError_t e = cudaFuncSetAttribute(radix_downsweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kDownsweepDyn);
+    if (e != cudaSuccess) return e;
+    attrSet = true;
+  }
   for (int shift = 0; shift < bits; shift += 8, passes++) {
     radix_upsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, n, shift, hist, (uint32_t)nTiles, nDev);
     g_launches++;
     cudaError_t e = scan_u32(hist, hist, nh, nullptr, scanSc, st);
     if (e != cudaSuccess) return e;
-    radix_downsweep_kernel<<<(unsigned)nTiles, kSortThreads, 0, st>>>(ks, vs, kd, vd, n, shift, hist,
-                                                                       (uint32_t)nTiles, nDev);
+    radix_downsweep_kernel<<<(unsigned)nTiles, kSortThreads, kDownsweepDyn, st>>>(ks, vs, kd, vd, n, shift, hist,
+                                                                                   (uint32_t)nTiles, nDev);
     g_launches++;
     unsigned long long *tk = ks; ks = kd; kd = tk;
     uint32_t *tv = vs; vs = vd; vd = tv;

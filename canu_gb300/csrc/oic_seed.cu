@@ -13,6 +13,12 @@
 // grouped by partner read with match_any, and the lowest lane of each group replays its
 // group's seeds in lane order.  Different partners advance in parallel; one partner's
 // seeds stay in order.  The pair table and node pool live in the warp's HBM scratch.
+//
+// A table probe is one 16-byte load of a (key, value) slot.  The qualifying
+// occurrences of a k-mer (partner ID above the ref read's) are the tail of its run,
+// which ascends by partner: runs of up to kScanMax entries are counted by a backward
+// scan, four entries per step -- the entries the replay reads next -- and longer runs
+// by binary search.
 #include "oic_kernels.cuh"
 #include "oic_prims.cuh"
 
@@ -22,6 +28,7 @@ namespace {
 
 constexpr int kSeedThreads = 128;
 constexpr int kSeedWarps   = kSeedThreads / 32;
+constexpr int kScanMax     = 64;   // occurrence runs up to this long are scanned backwards
 
 struct SeedSmem {
   u32 incl[32];
@@ -122,6 +129,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
       sm.overflow = 0;
     }
     bool lscr = false, rscr = false;
+    unsigned long long segSeeds = 0;   // counted once the segment completes in this configuration
     __syncwarp();
 
     for (int i0 = 0; i0 < nK; i0 += 32) {
@@ -142,15 +150,30 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
           } else {
             const u32 start = (u32)(val & 0xffffffffull);
             const u32 cnt   = (u32)((val >> 32) & 0x7fffffffull);
-            // first occurrence whose string is past thr (occurrences ascend by string)
-            u32 lo = start, hi = start + cnt;
-            while (lo < hi) {
-              u32 mid = (lo + hi) >> 1;
-              if ((i64)(T.occ[mid] >> 32) > thr) hi = mid;
-              else lo = mid + 1;
+            const u32 end   = start + cnt;
+            if (cnt <= (u32)kScanMax) {
+              while (n < cnt) {
+                u64 o[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) o[k] = (n + k < cnt) ? __ldg(T.occ + (end - 1 - n - k)) : 0ull;
+                u32 q = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                  if (q == (u32)k && n + k < cnt && (i64)(o[k] >> 32) > thr) q++;
+                n += q;
+                if (q < 4) break;
+              }
+            } else {
+              // first occurrence whose string is past thr
+              u32 lo = start, hi = end;
+              while (lo < hi) {
+                u32 mid = (lo + hi) >> 1;
+                if ((i64)(T.occ[mid] >> 32) > thr) hi = mid;
+                else lo = mid + 1;
+              }
+              n = end - lo;
             }
-            n    = start + cnt - lo;
-            qEnd = start + cnt;
+            qEnd = end;
           }
         }
       }
@@ -159,7 +182,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
       sm.incl[lane]   = incl;
       sm.qEnd[lane]   = qEnd;
       __syncwarp();
-      nSeeds += (lane == 0) ? total : 0;
+      segSeeds += (lane == 0) ? total : 0;
 
       for (u32 b = 0; b < total; b += 32) {
         const u32  s     = b + lane;
@@ -244,6 +267,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(ReadsDev R, TableDev
     __syncwarp();
     const int nPairs = min(sm.nPairs, cap.pairCap);
     const bool ovf   = sm.overflow != 0;
+    if (!ovf) nSeeds += segSeeds;
 
     if (!ovf && nPairs > 0) {
       // Node counts per pair, then one global allocation for the segment.
