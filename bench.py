@@ -477,6 +477,23 @@ def main():
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
     int_ops = 6 * cells + slides / 16.0
+    # The memory stages by the byte model of the hash build and probe: build 0.25 B per
+    # base read + 12 B per k-mer written (8 B key, 4 B position), and separately the sort
+    # passes (6 passes x 24 B per k-mer); probe 2 strands x (0.25 B per base + one 32 B
+    # sector per lookup) + 12 B per seed (4 B position read, 8 B seed written).
+    K = p.kmerLen
+    n_kmers = float(np.maximum(ln.astype(np.int64) - K + 1, 0).sum())
+    n_bases = float(ln.astype(np.int64).sum())
+    ms_hash = statistics.mean(r[0]["msHash"] for r in res)
+    ms_seed = statistics.mean(r[0]["msSeed"] for r in res)
+    sort_passes = (2 * K + 1 + 7) // 8
+
+    def stage_roof(nbytes, ms, basis):
+        ach = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else None
+        return {"achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"] if ach else None, "bytes": nbytes, "ms": ms, "basis": basis}
+    hash_bytes = 0.25 * n_bases + 12 * n_kmers
+    seed_bytes = 2 * n_bases * (0.25 + 32) + 12 * float(st0["seeds"])
     line = {
         "metric": "overlaps_per_sec", "value": value, "unit": "overlaps/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_dev_max, "higher_is_better": True, "scaling": "weak",
@@ -500,7 +517,11 @@ def main():
                      "int_ops": {"achieved_tops": int_ops / (ms_align / 1000.0) / 1e12, "peak_tops": int_peak,
                                  "frac": int_ops / (ms_align / 1000.0) / 1e12 / int_peak,
                                  "basis": "6 INT ops per DP cell + 1/16 per slide base; peak = 152 SMs x 128 "
-                                          "INT32 lanes x median SM clock"}},
+                                          "INT32 lanes x median SM clock"},
+                     "hash": stage_roof(hash_bytes, ms_hash, "0.25 B/base + 12 B/k-mer (sort passes excluded)"),
+                     "hash_with_sort": stage_roof(hash_bytes + sort_passes * 24 * n_kmers, ms_hash,
+                                                  f"as hash + {sort_passes} radix passes x 24 B/k-mer"),
+                     "seed": stage_roof(seed_bytes, ms_seed, "2 strands x (0.25 B/base + 32 B/lookup) + 12 B/seed")},
         "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in res)),
         "clocks": clk,
     }

@@ -30,7 +30,7 @@ EXPORTS = (
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
     "oic_extend_batch_noalloc", "oic_set_filter", "oic_collect_pairs", "oic_num_pairs", "oic_get_pairs",
     "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam", "oic_set_tuning", "oic_get_tuning",
-    "oic_autotune", "oic_count_kmers",
+    "oic_autotune", "oic_count_kmers", "oic_store_sort",
 )
 # Output files (include/oic_ovfile.h): host code of the same library, no GPU needed.
 OVFILE_EXPORTS = (
@@ -106,7 +106,8 @@ class OicTuning(ctypes.Structure):
     """oic_tuning: DP launch configuration (zeros = defaults)."""
     _fields_ = [("narrowArena", ctypes.c_uint32), ("wideMinLen", ctypes.c_uint32), ("wideThreads", ctypes.c_uint32),
                 ("wideTile", ctypes.c_uint32), ("wideBandW", ctypes.c_uint32), ("wideCtas", ctypes.c_uint32),
-                ("wideArena", ctypes.c_uint64), ("forceWide", ctypes.c_uint32), ("noGraph", ctypes.c_uint32)]
+                ("wideArena", ctypes.c_uint64), ("forceWide", ctypes.c_uint32), ("noGraph", ctypes.c_uint32),
+                ("wideMode", ctypes.c_uint32)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -139,6 +140,7 @@ def library():
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
+        lib.oic_store_sort.argtypes = [ctypes.c_int, vp, U64, U32, ctypes.c_double, vp, P(U64), vp, vp]
         lib.oic_ovb_write.argtypes = [ctypes.c_char_p, vp, U64, ctypes.c_int]
         lib.oic_ovb_read.argtypes = [ctypes.c_char_p, vp, U64, P(U64)]
         lib.oic_oc_path.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
@@ -452,6 +454,23 @@ def merge_outputs(out_ovb, inputs):
     """Merge independent jobs' .ovb/.oc outputs into out_ovb and its .oc."""
     arr = (ctypes.c_char_p * len(inputs))(*[os.fsencode(x) for x in inputs])
     _file_check(library().oic_merge_outputs(os.fsencode(out_ovb), arr, len(inputs)), "merge", out_ovb)
+
+
+def store_sort(records, max_id, max_erate=1.0, device=0):
+    """The overlap-store build's record pass on the GPU (oic_store_sort): returns (sorted
+    records (m, 6) uint32, perRead first-record offsets (max_id + 2) uint64, counters
+    dict)."""
+    r = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 6)
+    out = np.zeros((2 * len(r), 6), dtype=np.uint32)
+    per = np.zeros(int(max_id) + 2, dtype=np.uint64)
+    cnt = np.zeros(5, dtype=np.uint64)
+    m = ctypes.c_uint64()
+    rc = library().oic_store_sort(int(device), _ptr(r), len(r), int(max_id), float(max_erate), _ptr(out),
+                                  ctypes.byref(m), _ptr(per), _ptr(cnt))
+    if rc != OIC_OK:
+        raise OicError(rc, "oic_store_sort failed")
+    names = ("saved_unitigging", "saved_trimming", "discarded_erate", "discarded_no_trim", "discarded_flipped")
+    return out[: m.value], per, dict(zip(names, map(int, cnt)))
 
 
 def sort_records(rec):

@@ -9,6 +9,7 @@ Outputs (git-ignored) go to canu_gb300/_build/:
     oic_synth          the synthetic read generator
     oic_kmers          frequent k-mers of a read container (the -k skip file)
     oic_merge          merges the outputs of independent jobs (.ovb blocks, .oc counts)
+    oic_store_build    the overlap-store build's record pass: filter, swapped copies, sort
 
 Each translation unit is compiled in parallel; nvcc targets exactly sm_103a.
 """
@@ -29,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-O3",
            "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC]
 CU_SOURCES = ["oic_prims.cu", "oic_hash.cu", "oic_seed.cu", "oic_pairs.cu", "oic_capi.cu", "oic_noalloc.cu",
-              "oic_filter.cu", "oic_kmers.cu"]
+              "oic_filter.cu", "oic_kmers.cu", "oic_store.cu"]
 HOST_SOURCES = ["oic_ovfile.cpp"]   # canu_gb300/host: host-only parts of the library
 
 
@@ -105,7 +106,8 @@ def build_tools():
     nv = nvcc()
     cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
     lib = os.path.join(OUT, "liboic_gpu.so")
-    tools = {"overlapInCore": "overlapInCore.cpp", "oic_kmers": "oic_kmers.cpp", "oic_merge": "oic_merge.cpp"}
+    tools = {"overlapInCore": "overlapInCore.cpp", "oic_kmers": "oic_kmers.cpp", "oic_merge": "oic_merge.cpp",
+             "oic_store_build": "oic_store_build.cpp"}
     jobs = []
     for name, src in tools.items():
         s = os.path.join(HERE, "host", src)

@@ -381,6 +381,7 @@ oic_tuning resolved_tuning(const oic_ctx *c) {
   if (!t.wideTile) t.wideTile = 1;
   if (!t.wideBandW) t.wideBandW = 12288;
   if (!t.wideCtas) t.wideCtas = resolved_tuning_ctas(c, t);
+  if (!t.wideMode) t.wideMode = 2;
   return t;
 }
 
@@ -413,6 +414,64 @@ int ensure_group_scratch(oic_ctx *ctx, const oic_tuning &t, bool huge, uint32_t 
   ac.caps  = caps;
   if (ctx->dArena2.cap < (size_t)ctas * caps.arenaCap * sizeof(int)) ctx->dArena2.release();
   return ensure_align_scratch(ctx, ac, true, ws);
+}
+
+// The speculative CTA bin's scratch: 2 CTAs per SM (wideCtas when set) of
+// align_spec_warps() warps, each warp with the one-warp DP's scratch (512-int shared
+// rows, HBM rows up to 16384 diagonals, 32767 error rows) and an arena of the CTA's
+// wideArena cells (default: 40 % of the free memory, at most 2^27 cells per CTA) split
+// between its warps -- the heavy extensions of long high-error pairs keep millions of
+// cells each.
+int ensure_spec_scratch(oic_ctx *ctx, const oic_tuning &t, uint32_t &ctas, AlignCaps &caps, WarpScratch &ws) {
+  const int sw = align_spec_warps();
+  caps.rowCap  = 1 << 15;
+  caps.nodeCap = (1 << 22) / sw;   // a pair's alive flags take its CTA's warps' slots
+  caps.bandW   = 512;
+  caps.rowsGW  = 1 << 14;
+  ctas         = ctx->tune.wideCtas ? ctx->tune.wideCtas : (uint32_t)(2 * ctx->nSM);
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  freeB += ctx->dArena2.cap;
+  const size_t fixedPer = (size_t)sw * ((size_t)caps.rowCap * (16 + 12) + (size_t)caps.rowsGW * 8 + caps.nodeCap + 64);
+  uint64_t cells = t.wideArena;
+  if (!cells) {
+    double per = 0.4 * (double)freeB / ctas - (double)fixedPer;
+    cells      = per > 0 ? (uint64_t)(per / sizeof(int)) : 0;
+    cells      = std::min<uint64_t>(cells, 1ull << 27);
+  }
+  if (cells < (uint64_t)sw << 17) return fail(ctx, OIC_ERR_NOMEM, "not enough device memory for the CTA-bin DP arena");
+  caps.arenaCap = (int)std::min<uint64_t>(cells / sw, 0x7fff0000ull);
+  AlignConfig ac;
+  ac.bandW = caps.bandW;
+  ac.warps = (int)ctas * sw;
+  ac.caps  = caps;
+  if (ctx->dArena2.cap < (size_t)ac.warps * caps.arenaCap * sizeof(int)) ctx->dArena2.release();
+  return ensure_align_scratch(ctx, ac, true, ws);
+}
+
+// The CTA bin of a batch (its first level; the large-arena rerun is always CTA-wide).
+struct CtaBin {
+  bool        spec;
+  uint32_t    ctas;
+  AlignCaps   caps;
+  WarpScratch ws;
+};
+
+int ensure_cta_bin(oic_ctx *ctx, const oic_tuning &t, CtaBin &b) {
+  b.spec = t.wideMode != 2;
+  return b.spec ? ensure_spec_scratch(ctx, t, b.ctas, b.caps, b.ws)
+                : ensure_group_scratch(ctx, t, false, b.ctas, b.caps, b.ws);
+}
+
+void launch_cta_bin(oic_ctx *ctx, const oic_tuning &t, const CtaBin &b, uint32_t ctas, const uint32_t *work,
+                    uint32_t nWork, const AlignOut &ao, cudaStream_t s) {
+  if (b.spec)
+    launch_align_spec((int)ctas, ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(), work, nWork,
+                      ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), b.ws, b.caps, ao, s);
+  else
+    launch_align_group((int)t.wideThreads, (int)t.wideTile, b.caps.bandW, (int)ctas, ctx->R, ctx->T, ctx->dp,
+                       ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(), work, nWork, ctr32(ctx) + cWorkCounter,
+                       ctx->dNodes.as<int4>(), b.ws, b.caps, ao, s);
 }
 
 // Seed stage of a batch: the ref reads' seeds replayed into candidate pairs and match
@@ -616,15 +675,21 @@ int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning
       CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, sizeof(uint32_t), ctx->st));
       CK(cudaMemsetAsync(ctr32(ctx) + cAlnOvf, 0, sizeof(uint32_t), ctx->st));
       CK(cudaMemsetAsync(ctr32(ctx) + cErr, 0, sizeof(uint32_t), ctx->st));
-      uint32_t    ctas = 0;
-      AlignCaps   caps;
-      WarpScratch ws;
-      if ((rc = ensure_group_scratch(ctx, tn, huge, ctas, caps, ws))) return rc;
-      const int threads = huge ? (int)std::max<uint32_t>(tn.wideThreads, 512) : (int)tn.wideThreads;
-      launch_align_group(threads, (int)tn.wideTile, caps.bandW, (int)std::min<uint32_t>(ctas, nW), ctx->R, ctx->T,
-                         ctx->dp, ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(),
-                         ctx->dWork.as<uint32_t>() + nNarrow, nW, ctr32(ctx) + cWorkCounter,
-                         ctx->dNodes.as<int4>(), ws, caps, ao, ctx->st);
+      if (!huge) {
+        CtaBin b;
+        if ((rc = ensure_cta_bin(ctx, tn, b))) return rc;
+        launch_cta_bin(ctx, tn, b, std::min<uint32_t>(b.ctas, nW), ctx->dWork.as<uint32_t>() + nNarrow, nW, ao,
+                       ctx->st);
+      } else {
+        uint32_t    ctas = 0;
+        AlignCaps   caps;
+        WarpScratch ws;
+        if ((rc = ensure_group_scratch(ctx, tn, true, ctas, caps, ws))) return rc;
+        launch_align_group((int)std::max<uint32_t>(tn.wideThreads, 512), (int)tn.wideTile, caps.bandW,
+                           (int)std::min<uint32_t>(ctas, nW), ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(),
+                           ctx->dPairs.as<PairRec>(), ctx->dWork.as<uint32_t>() + nNarrow, nW,
+                           ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), ws, caps, ao, ctx->st);
+      }
       CK(cudaMemcpyAsync(h, ctx->dCtr.p, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->st));
       if ((rc = sync_check(ctx, huge ? "align kernel (large arena)" : "align kernel (CTA bin)"))) return rc;
       at.pairsWide += nW;
@@ -729,10 +794,11 @@ int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_
   an.caps.arenaCap = (int)tn.narrowArena;
   WarpScratch wsN;
   if ((rc = ensure_align_scratch(ctx, an, false, wsN))) return rc;
-  uint32_t    ctas = 0;
-  AlignCaps   capsG;
-  WarpScratch wsG;
-  if ((rc = ensure_group_scratch(ctx, tn, false, ctas, capsG, wsG))) return rc;
+  CtaBin bG;
+  if ((rc = ensure_cta_bin(ctx, tn, bG))) return rc;
+  const uint32_t    ctas  = bG.ctas;
+  const AlignCaps   capsG = bG.caps;
+  const WarpScratch wsG   = bG.ws;
   for (cudaEvent_t &e : ctx->gEv)
     if (!e) CK(cudaEventCreate(&e));
 
@@ -754,8 +820,6 @@ int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_
   aoW.nWorkDev   = ctr32(ctx) + cWideN;   // CTA bin: work[bin 0 .. bin 0 + wideN)
   aoW.workOffDev = ctr32(ctx) + cKeep;
   const float *logit = useFilter ? ctx->dLogit.as<float>() : nullptr;
-  const int    threads = (int)tn.wideThreads;
-
   std::vector<uint8_t> key;
   key_add(key, aoN);
   key_add(key, aoW);
@@ -807,9 +871,7 @@ int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_
     launch_append_overflow(ctx->dWork.as<uint32_t>(), ctr32(ctx) + cKeep, ctx->dAlnOvf.as<uint32_t>(),
                            ctr32(ctx) + cAlnOvf, ctr32(ctx) + cWideN, ctr32(ctx) + cWorkCounter, ctr32(ctx) + cErr,
                            s);
-    launch_align_group(threads, (int)tn.wideTile, capsG.bandW, (int)ctas, ctx->R, ctx->T, ctx->dp,
-                       ctx->dEml.as<int>(), ctx->dPairs.as<PairRec>(), ctx->dWork.as<uint32_t>(), 0,
-                       ctr32(ctx) + cWorkCounter, ctx->dNodes.as<int4>(), wsG, capsG, aoW, s);
+    launch_cta_bin(ctx, tn, bG, ctas, ctx->dWork.as<uint32_t>(), 0, aoW, s);
     cudaEventRecordWithFlags(ctx->gEv[2], s, cudaEventRecordExternal);   // recorded at every replay
     scan_u32(ctx->dCnt.as<uint32_t>(), ctx->dRecPos.as<uint32_t>(), cap, ctr32(ctx) + cRecTotal,
              ctx->dScanScratch.p, s);
@@ -1903,12 +1965,21 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
   };
   auto total = [](const Line &l) { return (double)l.at.msNarrow + l.at.msWide; };
   if (!rc && nPairs) {
-    // Stage 1: warps per pair x tile width of the CTA bin, no length bin.
+    // Stage 1: the speculative CTA bin, then CTA-wide rows with warps per pair x tile
+    // width, no length bin.
+    {
+      oic_tuning t = base;
+      t.wideMode   = 1;
+      t.wideMinLen = 0xffffffffu;
+      rc           = measure(t);
+    }
     const uint32_t threadsGrid[] = {64, 128, 256, 512};
     const uint32_t tileGrid[]    = {1, 2, 4};
     for (uint32_t th : threadsGrid)
       for (uint32_t tl : tileGrid) {
+        if (rc) break;
         oic_tuning t  = base;
+        t.wideMode    = 2;
         t.wideThreads = th;
         t.wideTile    = tl;
         t.wideMinLen  = 0xffffffffu;
@@ -1949,8 +2020,8 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
     ctx->tune = lines[best].t;
     if (verbose())
       for (const Line &l : lines)
-        fprintf(stderr, "oic: autotune: threads %u tile %u length bin %d: one-warp %.1f ms, CTA %.1f ms\n",
-                l.t.wideThreads, l.t.wideTile, l.t.wideMinLen == 0xffffffffu ? -1 : (int)l.t.wideMinLen,
+        fprintf(stderr, "oic: autotune: %s threads %u tile %u length bin %d: one-warp %.1f ms, CTA %.1f ms\n",
+                l.t.wideMode == 2 ? "CTA rows" : "speculative", l.t.wideThreads, l.t.wideTile, l.t.wideMinLen == 0xffffffffu ? -1 : (int)l.t.wideMinLen,
                 l.at.msNarrow, l.at.msWide);
     if (verbose())
       fprintf(stderr, "oic: autotune: %zu configurations on %u pairs; best: %u threads, tile %u, length bin %u (%.1f ms)\n",
@@ -1961,7 +2032,7 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
   for (const Line &l : lines) {
     if (!report || k >= maxReport) break;
     double *r = report + (size_t)k * 8;
-    r[0] = l.t.wideTile;
+    r[0] = l.t.wideMode == 2 ? l.t.wideTile : 0;
     r[1] = l.t.wideThreads;
     r[2] = l.t.wideMinLen == 0xffffffffu ? -1.0 : (double)l.t.wideMinLen;
     r[3] = l.at.msNarrow;

@@ -127,6 +127,16 @@ void launch_align_group(int threads, int U, int bandW, int ctas, ReadsDev R, Tab
                         const PairRec *pairs, const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes,
                         WarpScratch sc, AlignCaps cap, AlignOut out, cudaStream_t st);
 
+// Speculative CTA bin: one pair per CTA of align_spec_warps() warps, each warp running
+// whole extensions (one-warp DP, 512-int shared-memory rows, HBM rows up to
+// cap.rowsGW) of the pair's next alive match nodes, replayed in the reference's order.
+// sc/cap describe ctas * align_spec_warps() warp scratches; a pair's alive flags use the
+// nodeCap bytes of all its CTA's warps.
+void launch_align_spec(int ctas, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs,
+                       const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap,
+                       AlignOut out, cudaStream_t st);
+int align_spec_warps();
+
 struct ExtendProblem;
 void launch_extend_group(int threads, int U, int bandW, int ctas, ReadsDev R, DevParams P, const int *eml,
                          const ExtendProblem *probs, u32 n, WarpScratch sc, AlignCaps cap, int *out, int *kind,

@@ -522,6 +522,344 @@ __global__ void __launch_bounds__(512, 1) align_group_kernel(ReadsDev R, TableDe
   group_bar(1, blockDim.x);
 }
 
+// ---------------------------------------------------------------------------------
+// Speculative CTA bin: one pair per CTA of kSpecWarps warps, each warp running whole
+// extensions with the one-warp DP.  Process_Matches extends, one after another, the
+// longest alive match node (first in list order on ties) and then removes the nodes
+// that lie on its alignment (Process_String_Overlaps.C:420-491).  An extension depends
+// only on its own node, and removal only ever takes nodes away, so the order of
+// extensions is the order of the nodes by (length descending, list index ascending),
+// skipping removed nodes.  Each round, warp 0 picks the next kSpecWarps alive nodes in
+// that order, every warp extends one of them, and warp 0 replays the round in order:
+// a node removed by an earlier extension of the round is skipped (its result is
+// discarded), the others are committed exactly as the sequential loop commits them.
+// Only committed extensions count as DP work.  Consistent pairs (a single extension)
+// and pairs under the filter's extension budget take one node per round.
+constexpr int kSpecWarps = 8;
+enum { kSpecExtend = 1, kSpecExit = 2 };
+
+struct SpecRes {
+  int sLo, sHi, tLo, tHi, errors, kind, leftLen;
+  u32 err;
+  unsigned long long cells, slides, rows;
+};
+
+struct SpecShared {
+  int         cmd;
+  int         nCand;
+  int         cand[kSpecWarps];
+  SeqView     S, T;
+  int         sLen, tLen;
+  const int4 *nodes;
+  SpecRes     res[kSpecWarps];
+};
+
+// Warp `wib` extends node cand[wib] of the posted pair into res[wib]; its deltas stay
+// in its scratch (sc.deltaL) until the next round.
+static __device__ __forceinline__ void spec_work(WarpDP &w, SpecShared &ss, int wib) {
+  const int lane = threadIdx.x & 31;
+  if (wib >= ss.nCand) return;
+  const int4 lm = ss.nodes[ss.cand[wib]];
+  const unsigned long long c0 = w.cells, r0 = w.rows, s0 = w.slides;
+  w.err = 0;
+  int sLo = 0, sHi = 0, tLo = 0, tHi = 0, errors = 0;
+  const int kind = warp_extend<false>(w, ss.S, ss.sLen, ss.T, ss.tLen, lm.z, lm.x, lm.y, sLo, sHi, tLo, tHi, errors);
+  const unsigned long long sl = warp_sum64(w.slides - s0);
+  if (lane == 0) {
+    SpecRes &r = ss.res[wib];
+    r.sLo = sLo; r.sHi = sHi; r.tLo = tLo; r.tHi = tHi; r.errors = errors; r.kind = kind;
+    r.leftLen = w.leftLen;
+    r.err     = w.err;
+    r.cells   = w.cells - c0;
+    r.rows    = w.rows - r0;
+    r.slides  = sl;
+  }
+  __syncwarp();
+}
+
+// Process_Matches for one pair on warp 0 of a speculative CTA (same rules and outputs as
+// process_pair); wsc[j] is warp j's scratch (for its deltas).  Committed DP work is
+// added to ps.pc.  Returns false on a capacity overflow.
+__device__ bool process_pair_spec(WarpDP &w, PairSmem &ps, SpecShared &ss, const WarpScratch *wsc, int nThr,
+                                  const ReadsDev &R, const TableDev &Tb, const PairRec &pr, const int4 *nodesAll,
+                                  u32 *recOut, u32 &nRec, int extLimit, unsigned long long &cellsPair) {
+  const int lane = threadIdx.x & 31;
+  const DevParams &P = w.P;
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kStCount; i++) ps.pc.v[i] = 0;
+    ps.nOlap      = 0;
+    ps.nExt       = 0;
+    ps.firstHit   = -1;
+    ps.cellsFirst = 0;
+  }
+  __syncwarp();
+  nRec      = 0;
+  cellsPair = 0;
+
+  const u32 sRead = pr.sRead;
+  const int rev   = pr.flags & 1;
+  const int cons  = (pr.flags >> 1) & 1;
+  const bool segL = (pr.flags >> 2) & 1, segR = (pr.flags >> 3) & 1;
+  const int sLen  = (int)R.len[sRead];
+  const u32 tRead = Tb.sread[pr.tStr];
+  const int tLen  = (int)R.len[tRead];
+
+  // --minkmers (computeMinimumKmers, Process_String_Overlaps.C:21-33, :618-621)
+  if (P.minKmers) {
+    double ol = (double)(pr.diagEnd - pr.diagBgn);
+    if (ol < 0) ol = -ol;
+    unsigned long long ex = 0;
+    if (!(ol < (double)P.kmerLen))
+      ex = (unsigned long long)(long long)(int)floor(
+          __dmul_rn(P.kmerExpect, __dadd_rn(__dsub_rn(ol, (double)P.kmerLen), 1.0)));
+    const unsigned long long need = P.minKmers > ex ? P.minKmers : ex;
+    if (need > (unsigned long long)(long long)pr.diagCt) {
+      if (lane == 0) ps.pc.v[kStSkipped] = 1;
+      __syncwarp();
+      return true;
+    }
+  }
+
+  const int4 *nodes = nodesAll + pr.nodeOff;
+  const int   cnt   = (int)pr.nodeCnt;
+  if (cnt <= 0) {
+    if (lane == 0) ps.pc.v[kStWithoutOlap] = 1;
+    __syncwarp();
+    return true;
+  }
+
+  // Hopeless check for a single match (:384-415).
+  if (P.hopeless && cnt == 1 && !P.partial) {
+    const int4 m = nodes[0];
+    const bool tLs = Tb.lscr[pr.tStr] != 0, tRs = Tb.rscr[pr.tStr] != 0;
+    bool hopeless = false;
+    const int sHead = m.z, tHead = m.x;
+    if (sHead <= tHead) {
+      if (sHead > kHopelessMatch && !segL) hopeless = true;
+    } else {
+      if (tHead > kHopelessMatch && !tLs) hopeless = true;
+    }
+    const int sTail = sLen - sHead - m.y + 1, tTail = tLen - tHead - m.y + 1;
+    if (sTail <= tTail) {
+      if (sTail > kHopelessMatch && !segR) hopeless = true;
+    } else {
+      if (tTail > kHopelessMatch && !tRs) hopeless = true;
+    }
+    if (hopeless) {
+      if (lane == 0) ps.pc.v[kStWithoutOlap] = 1;
+      __syncwarp();
+      return true;
+    }
+  }
+
+  if (cnt > w.cap.nodeCap) {
+    w.err |= kErrNodesPerPair;
+    return false;
+  }
+  // alive: 1 alive, 2 alive and picked for the current round, 0 removed.
+  unsigned char *alive = w.sc.alive;
+  for (int i = lane; i < cnt; i += 32) alive[i] = 1;
+  if (lane == 0) {
+    ss.S     = make_view(R, sRead, rev);
+    ss.T     = make_view(R, tRead, 0);
+    ss.sLen  = sLen;
+    ss.tLen  = tLen;
+    ss.nodes = nodes;
+  }
+  __syncwarp();
+  const int want = (cons || extLimit > 0) ? 1 : kSpecWarps;
+  bool done = false, failed = false;
+
+  while (!done) {
+    // The next `want` alive nodes by (length descending, list index ascending).
+    int nC = 0;
+    for (; nC < want; nC++) {
+      int myLen = -1, myIdx = INT_MAX;
+      for (int i = lane; i < cnt; i += 32)
+        if (alive[i] == 1) {
+          const int len = nodes[i].y;
+          if (len > myLen) {
+            myLen = len;
+            myIdx = i;
+          }
+        }
+      const int maxLen = __reduce_max_sync(0xffffffffu, myLen);
+      if (maxLen < 0) break;
+      const int li = __reduce_min_sync(0xffffffffu, myLen == maxLen ? myIdx : INT_MAX);
+      if (lane == 0) {
+        alive[li]   = 2;
+        ss.cand[nC] = li;
+      }
+      __syncwarp();
+    }
+    if (nC == 0) break;
+    if (lane == 0) {
+      ss.nCand = nC;
+      ss.cmd   = kSpecExtend;
+    }
+    __syncwarp();
+    group_bar(1, nThr);
+    spec_work(w, ss, 0);
+    group_bar(2, nThr);
+
+    for (int j = 0; j < nC; j++) {
+      const int li = ss.cand[j];
+      if (alive[li] != 2) continue;            // removed by an earlier extension of the round
+      const SpecRes &r = ss.res[j];
+      if (r.err) {
+        w.err |= r.err;
+        failed = true;
+        done   = true;
+        break;
+      }
+      cellsPair += r.cells;
+      const bool dov = (r.kind == kDovetail) || P.partial;
+      if (lane == 0) {
+        ps.pc.v[kStExtensions]++;
+        ps.pc.v[kStCells] += r.cells;
+        ps.pc.v[kStSlides] += r.slides;
+        ps.pc.v[kStRows] += r.rows;
+        bool added = false;
+        if (dov && 1 + r.sHi - r.sLo >= P.minOlapLen && 1 + r.tHi - r.tLo >= P.minOlapLen) {
+          const int    olapLen = 1 + min(r.sHi - r.sLo, r.tHi - r.tLo);
+          const double quality = __ddiv_rn((double)r.errors, (double)olapLen);
+          if (r.errors <= error_bound(olapLen, P.maxErate)) {
+            add_overlap(P.partial, r.sLo, r.sHi, r.tLo, r.tHi, quality, r.leftLen, ps.olap, ps.nOlap);
+            added = true;
+          }
+        }
+        if (ps.nExt == 0) ps.cellsFirst = r.cells;
+        if (added && ps.firstHit < 0) ps.firstHit = ps.nExt;
+        ps.nExt++;
+      }
+      __syncwarp();
+      if (cons) { done = true; break; }
+      if (extLimit > 0 && ps.nExt >= extLimit && ps.nOlap == 0) { done = true; break; }
+      // Drop the extended node and every node that lies on its alignment (:476-490).
+      const int *dl = wsc[j].deltaL;
+      for (int i = lane; i < cnt; i += 32) {
+        if (!alive[i]) continue;
+        const int4 q = nodes[i];
+        bool rm = (i == li);
+        if (!rm && dov && r.sLo - kShiftSlack <= q.z && q.z + q.y <= (r.sHi + 1) + kShiftSlack - 1 &&
+            lies_on_alignment(dl, r.leftLen, q.z, q.x, r.sLo, r.tLo))
+          rm = true;
+        if (rm) alive[i] = 0;
+      }
+      __syncwarp();
+    }
+  }
+  if (failed) return false;
+
+  if (lane == 0) {
+    const u32 sID = sRead + 1, tID = tRead + 1;
+    int nOut = 0;
+    const int nOlap = ps.nOlap;
+    if (nOlap > 0) {
+      int deleted[kMaxDistinct] = {0, 0, 0};
+      if (P.partial) {
+        if (P.unique) choose_best_partial(ps.olap, nOlap, deleted);
+      } else {
+        if (P.unique) combine_into_one(ps.olap, nOlap, deleted);
+        else merge_intersecting(ps.olap, nOlap, deleted);
+      }
+      for (int i = 0; i < nOlap; i++)
+        if (!deleted[i]) {
+          if (P.partial) output_partial(recOut + nOut * 6, sID, tID, rev, ps.olap[i], sLen, tLen, ps.pc);
+          else output_overlap(recOut + nOut * 6, sID, sLen, rev, tID, tLen, ps.olap[i], ps.pc);
+          nOut++;
+        }
+    }
+    if (nOut == 0) ps.pc.v[kStWithoutOlap]++;
+    else {
+      ps.pc.v[kStWithOlap]++;
+      if (nOut > 1) ps.pc.v[kStMulti]++;
+    }
+    nRec = (u32)nOut;
+  }
+  __syncwarp();
+  return true;
+}
+
+// The speculative CTA bin (see above): warp 0 takes pairs from the work list and runs
+// their pair logic; all kSpecWarps warps run the extensions of each round.  Warp j's
+// scratch is scBase's warp blockIdx.x * kSpecWarps + j; the pair's alive flags are in
+// the nodeCap * kSpecWarps bytes that start at warp 0's.
+__global__ void __launch_bounds__(kSpecWarps * 32, OIC_ALIGN_MIN_BLOCKS) align_spec_kernel(
+    ReadsDev R, TableDev Tb, DevParams P, const int *eml, const PairRec *pairs, const u32 *work, u32 nWork,
+    u32 *workCounter, const int4 *nodes, WarpScratch scBase, AlignCaps cap, AlignOut out) {
+  extern __shared__ int smemRows[];
+  __shared__ PairSmem    ps;
+  __shared__ SpecShared  ss;
+  __shared__ WarpScratch wsc[kSpecWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nThr = blockDim.x;
+  const u64 gw = (u64)blockIdx.x * kSpecWarps + wib;
+  WarpDP w;
+  int *smA = smemRows + (size_t)wib * 2 * 512;
+  warp_dp_init(w, warp_scratch(scBase, cap, gw), cap, smA, smA + 512, eml, P);
+  if (lane == 0) wsc[wib] = w.sc;
+  w.cap.nodeCap = cap.nodeCap * kSpecWarps;   // warp 0's alive flags span the CTA's slots
+  __syncthreads();
+
+  if (wib != 0) {
+    while (true) {
+      group_bar(1, nThr);
+      if (ss.cmd != kSpecExtend) break;
+      spec_work(w, ss, wib);
+      group_bar(2, nThr);
+    }
+    return;
+  }
+
+  // Warp 0: the pairs.
+  if (out.nWorkDev) nWork = *out.nWorkDev;
+  if (out.workOffDev) work += *out.workOffDev;
+  if (lane == 0)
+    for (int i = 0; i < kStCount; i++) ps.acc.v[i] = 0;
+  __syncwarp();
+  while (true) {
+    u32 k = 0;
+    if (lane == 0) k = atomicAdd(workCounter, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= nWork) break;
+    const u32 pi = work[k];
+    const PairRec pr = pairs[pi];
+    u32 nRec = 0;
+    w.err = 0;
+    int extLimit = 0;
+    if (out.tierLogit && out.tierLogit[pi] < out.tierThr) extLimit = out.tierBudget;
+    unsigned long long cellsPair = 0;
+    const bool ok = process_pair_spec(w, ps, ss, wsc, nThr, R, Tb, pr, nodes, out.rec + (u64)pi * 18, nRec, extLimit,
+                                      cellsPair);
+    if (lane == 0) {
+      if (ok) {
+        if (nRec == 0) ps.pc.v[kStCellsNoOlap] += cellsPair;
+        out.cnt[pi] = nRec;
+        if (out.cells) {
+          out.cells[pi] = cellsPair > 0xffffffffull ? 0xffffffffu : (u32)cellsPair;
+          out.ext[pi]   = make_int4(ps.nExt, ps.firstHit,
+                                    ps.cellsFirst > 0x7fffffffull ? 0x7fffffff : (int)ps.cellsFirst, extLimit);
+        }
+        for (int i = 0; i < kStCount; i++) ps.acc.v[i] += ps.pc.v[i];
+      } else {
+        out.cnt[pi] = 0;
+        u32 slot = atomicAdd(out.overflowCount, 1u);
+        out.overflow[slot] = pi;
+        atomicOr(out.err, w.err);
+      }
+    }
+    __syncwarp();
+  }
+  if (lane == 0) {
+    ss.cmd = kSpecExit;
+    for (int i = 0; i < kStCount; i++)
+      if (ps.acc.v[i]) atomicAdd(&out.stats[i], ps.acc.v[i]);
+  }
+  __syncwarp();
+  group_bar(1, nThr);
+}
+
 // Work list order: key = bin << 30 | (2^30 - 1 - match nodes), value = pair index, so
 // the pairs sort by bin and, inside a bin, the pairs with the most match nodes (the most
 // extensions) come first.  Bin 0: the one-warp DP; bin 1: the CTA DP, for pairs whose
@@ -623,6 +961,21 @@ void launch_align_group(int threads, int U, int bandW, int ctas, ReadsDev R, Tab
                                                   U);
   g_launches++;
 }
+
+void launch_align_spec(int ctas, ReadsDev R, TableDev T, DevParams P, const int *eml, const PairRec *pairs,
+                       const u32 *work, u32 nWork, u32 *workCounter, const int4 *nodes, WarpScratch sc, AlignCaps cap,
+                       AlignOut out, cudaStream_t st) {
+  if (nWork == 0 && !out.nWorkDev) return;
+  cap.bandW         = 512;
+  cap.rowsGW        = cap.rowsGW < 512 ? 512 : cap.rowsGW;
+  const size_t smem = (size_t)kSpecWarps * 2 * 512 * sizeof(int);
+  cudaFuncSetAttribute(align_spec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  align_spec_kernel<<<ctas, kSpecWarps * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap,
+                                                        out);
+  g_launches++;
+}
+
+int align_spec_warps() { return kSpecWarps; }
 
 void launch_extend_batch(int, ReadsDev R, DevParams P, const int *eml, const ExtendProblem *probs, u32 n,
                          WarpScratch sc, AlignCaps cap, int nWarps, int *out, int *kind, int *deltaLen, u32 *status,

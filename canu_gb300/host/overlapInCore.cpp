@@ -17,7 +17,7 @@
 //     unframed instead of in snappy blocks (--ovb-snappy, the default, is accepted);
 //   * --gpu-tune key=value[,key=value...] sets DP launch fields of oic_tuning
 //     (narrowArena, wideMinLen, wideThreads, wideTile, wideBandW, wideCtas, wideArena,
-//     forceWide, noGraph), and --gpu-autotune <n> times the DP grid on the first n ref reads
+//     forceWide, noGraph, wideMode), and --gpu-autotune <n> times the DP grid on the first n ref reads
 //     against the first hash block and keeps the fastest configuration (oic_autotune).
 //     Neither changes the records.
 #include <cerrno>
@@ -122,6 +122,7 @@ bool parseTuning(const char *s, oic_tuning &t) {
     else if (k == "wideArena") t.wideArena = v;
     else if (k == "forceWide") t.forceWide = (uint32_t)v;
     else if (k == "noGraph") t.noGraph = (uint32_t)v;
+    else if (k == "wideMode") t.wideMode = (uint32_t)v;
     else return false;
     if (q == std::string::npos) break;
     p = q + 1;

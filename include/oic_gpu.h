@@ -274,6 +274,10 @@ typedef struct oic_tuning {
   uint32_t forceWide;     /* testing: every pair goes to the CTA bin (0 / 1) */
   uint32_t noGraph;       /* 1: launch the DP stage kernel by kernel with host-read sizes instead of
                              relaunching its captured CUDA graph (same records) */
+  uint32_t wideMode;      /* CTA bin kernel: 2 (default) CTA-wide rows (wideThreads, wideTile, wideBandW
+                             apply); 1 speculative -- the CTA's 8 warps each extend one of the pair's next
+                             alive match nodes with the one-warp DP and warp 0 replays them in the
+                             reference's order (wideArena is split between the warps) */
 } oic_tuning;
 
 int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t);   /* NULL: defaults */
@@ -281,14 +285,16 @@ int oic_get_tuning(oic_ctx *ctx, oic_tuning *t);          /* the configuration i
 
 /* Autotuner: runs the seed pass for ref reads [bgnRefID, endRefID] against the loaded
  * hash block once, then times the DP of those candidate pairs under each configuration
- * of a grid -- wideTile {1, 2, 4} x warps per pair {1 (one-warp bin only), 2, 4, 8} x
- * length-bin boundary {none, 4 quantiles of the pairs' shorter read} -- checks that
+ * of a grid -- the speculative CTA bin, then CTA-wide rows with wideTile {1, 2, 4} x
+ * warps per pair {2, 4, 8, 16} -- and then the best of those with length-bin boundary
+ * {none, 4 quantiles of the pairs' shorter read}, checks that
  * every configuration emits the same records, and sets the fastest (a length bin only
  * when it beats the best configuration without one by more than 5 %).  The sample's
  * DP runs once per configuration (16 times): keep it to a few seconds of DP.  With report
  * non-NULL, fills report[0 .. maxReport) with one line per configuration:
  * (wideTile, wideThreads, wideMinLen, narrow ms, wide ms, total ms, narrow cells,
- * wide cells) as doubles, and *nReport with the number of lines. */
+ * wide cells) as doubles (wideTile 0: the speculative CTA bin), and *nReport with the
+ * number of lines. */
 int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *report, uint32_t maxReport,
                  uint32_t *nReport);
 
@@ -302,6 +308,22 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
  * maxKmers: OIC_ERR_OVERFLOW, call again with room).  At most 2^32-2 windows. */
 int oic_count_kmers(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t minCount, char *kmers, uint32_t *counts,
                     uint64_t maxKmers, uint64_t *nKmers);
+
+/* The record pass of the overlap-store build (ovStoreBuild, src/stores/ovStoreBuild.C:
+ * 166-255) on CUDA device `device`: every record of words[0 .. 6 * nRecords) is checked
+ * (a_iid and b_iid in 1..maxID, else OIC_ERR_INPUT) and filtered as
+ * ovStoreFilter::filterOverlap does (src/stores/ovStoreFilter.C:62-160: a record whose
+ * evalue exceeds AS_OVS_encodeEvalue(maxErate) loses forUTG, forOBT and forDUP), its
+ * ID-swapped copy is made (ovOverlap::swapIDs, src/stores/ovOverlap.C:216-246), the
+ * record and the copy are kept when one of the three flags is set, and the kept records
+ * are sorted in ovOverlap order (a_iid, b_iid, the two data words) into out (room for
+ * 2 * nRecords records).  *nOut gets their number.  perRead (optional, maxID + 2
+ * entries): perRead[i] = index in out of the first record with a_iid i, perRead[maxID +
+ * 1] = *nOut.  counts (optional, 5): saved unitigging, saved trimming, discarded for
+ * the error rate, discarded untrimmed, discarded flipped -- ovStoreFilter's counters.
+ * Host buffers; the call allocates its device memory and returns when done. */
+int oic_store_sort(int device, const uint32_t *words, uint64_t nRecords, uint32_t maxID, double maxErate,
+                   uint32_t *out, uint64_t *nOut, uint64_t *perRead, uint64_t *counts);
 
 /* Edit_Match_Limit / Error_Bound tables the context uses (for testing): copies
  * min(n, table length) entries; *len gets the table length. */

@@ -167,6 +167,11 @@ public:
     if (oic_seqdb_load(path, &_db) != 0)
       fprintf(stderr, "Failed to load read container '%s'\n", path), exit(1);
   }
+  // A store that only knows its read count (the overlap-store oracle, oracle/store_ref.C).
+  sqStore(const char *, uint32 nReads) {
+    memset(&_db, 0, sizeof(_db));
+    _db.nReads = nReads;
+  }
   ~sqStore() { oic_seqdb_free(&_db); }
 
   uint32 sqStore_lastReadID(void) { return _db.nReads; }

@@ -1,6 +1,9 @@
-"""The CTA-bin DP (several warps per read pair, U diagonals per thread) and the
-autotuner: same alignments as the oracle, same records as the reference."""
+"""The CTA-bin DP -- speculative (every warp of the CTA extends one of the pair's next
+match nodes, replayed in the reference's order) and CTA-wide rows (several warps per
+row, U diagonals per thread) -- and the autotuner: same alignments as the oracle, same
+records as the reference."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -41,11 +44,13 @@ def test_cta_dp_matches_oracle(threads, tile, case, erate, partial, built, oracl
     plib.oic_port_aligner_free(al)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("name", sorted(golden_cases()))
-def test_cta_bin_matches_reference(name, built, golden_inputs, tmp_path):
-    """Every pair through the CTA bin: records, .oc and stats equal the reference's."""
+def test_cta_bin_matches_reference(name, mode, built, golden_inputs, tmp_path):
+    """Every pair through the CTA bin (1 speculative, 2 CTA-wide rows): records, .oc and
+    stats equal the reference's."""
     g = golden_inputs[name]
-    tune = f"forceWide=1,wideThreads=128,wideTile=2,wideArena={SMALL_ARENA},wideCtas=64"
+    tune = f"forceWide=1,wideMode={mode},wideThreads=128,wideTile=2,wideArena={SMALL_ARENA},wideCtas=64"
     rec, oc, st, log = run_cli(built["cli"], g["args"], g["db"], g["skip"], str(tmp_path), extra=["--gpu-tune", tune])
     grec, goc, gst = load_golden(name)
     assert rec.shape == grec.shape, log[-2000:]
@@ -88,12 +93,42 @@ def test_autotune_reports_the_grid_and_keeps_records(built, golden_inputs):
 
     base, _, _ = run(False)
     recs, lines, tun = run(True)
-    assert len(lines) == 16                      # 4 warps-per-pair x 3 tiles, then 4 length bins
-    assert {(l["wideThreads"], l["wideTile"]) for l in lines[:12]} == {(t, u) for t in (64, 128, 256, 512)
-                                                                        for u in (1, 2, 4)}
+    assert len(lines) == 17     # speculative, 4 warps-per-pair x 3 tiles of CTA rows, then 4 length bins
+    assert lines[0]["wideTile"] == 0
+    assert {(l["wideThreads"], l["wideTile"]) for l in lines[1:13]} == {(t, u) for t in (64, 128, 256, 512)
+                                                                         for u in (1, 2, 4)}
     best = min(lines, key=lambda l: l["msTotal"])
-    assert tun["wideThreads"] == best["wideThreads"] and tun["wideTile"] == best["wideTile"]
+    if best["wideTile"] == 0:
+        assert tun["wideMode"] == 1
+    else:
+        assert tun["wideMode"] == 2 and tun["wideThreads"] == best["wideThreads"] and tun["wideTile"] == best["wideTile"]
     assert np.array_equal(recs, base)
+
+
+@pytest.mark.parametrize("name", ["hierr", "hierr_partial", "multi", "repeats_noskip"])
+def test_speculative_bin_counts_only_the_reference_extensions(name, built, golden_inputs):
+    """Extensions whose node an earlier extension of the same round removed are
+    discarded: the speculative CTA bin reports exactly the DP work of the sequential
+    loop (extensions, DP cells, rows, slide bases) and the same records."""
+    g = golden_inputs[name]
+    args = g["args"].format(db=g["db"], skip=g["skip"] or "").split()
+
+    def opt(flag, default=None):
+        return args[args.index(flag) + 1] if flag in args else default
+    kw = dict(kmerLen=22, hashBits=16, maxHashLoad=0.8, maxErate=float(opt("--maxerate")),
+              minOlapLen=int(opt("--minlength")), partial=int("-partial" in args),
+              uniqueOlapPerPair=0 if "-m" in args else 1, numThreads=int(opt("-t")))
+    out = []
+    for mode in (1, 2):
+        with oic.Overlapper(oic.default_params(**kw)) as ov:
+            ov.set_reads_seqdb(g["db"])
+            ov.set_tuning(forceWide=1, wideMode=mode, wideArena=SMALL_ARENA, wideCtas=64)
+            ov.run()
+            out.append((oic.sort_records(ov.overlaps()), ov.stats()))
+    (ra, sa), (rb, sb) = out
+    assert len(ra) > 0 and np.array_equal(ra, rb)
+    for k in ("extensions", "dpCells", "dpRows", "slideBases", "totalOverlaps", "kmerHitsWithOlap"):
+        assert sa[k] == sb[k], (k, sa[k], sb[k])
 
 
 def test_captured_graph_matches_kernel_by_kernel(built, tmp_path_factory):
