@@ -1809,76 +1809,123 @@ int oic_count_kmers(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t minCo
   if (bgnID < 1) bgnID = 1;
   if (endID > ctx->nReads) endID = ctx->nReads;
   std::vector<uint32_t> reads;
-  std::vector<uint64_t> flat(1, 0);
+  uint64_t              n = 0;
   for (uint64_t id = bgnID; id <= endID; id++) {
     const uint32_t r = (uint32_t)id - 1;
     if (ctx->len[r] < (uint32_t)K) continue;
     reads.push_back(r);
-    flat.push_back(flat.back() + ctx->len[r] - K + 1);
+    n += ctx->len[r] - K + 1;
   }
-  const uint64_t n = flat.back();
-  *nKmers          = 0;
+  *nKmers = 0;
   if (n == 0) return OIC_OK;
-  if (n >= 0xfffffffeull) return fail(ctx, OIC_ERR_OVERFLOW, "more than 2^32-2 k-mer windows");
-  DevBuf dReads, dFlat, dK, dV, dK2, dV2, dScr, dFlags, dPos, dRun, dSel, dSelPos, dOutK, dOutC;
+  const uint32_t nr = (uint32_t)reads.size();
+  DevBuf dReads, dHist, dK, dV, dK2, dV2, dScr, dFlags, dPos, dRun, dSel, dSelPos, dOutK, dOutC;
   auto release = [&]() {
-    for (DevBuf *b : {&dReads, &dFlat, &dK, &dV, &dK2, &dV2, &dScr, &dFlags, &dPos, &dRun, &dSel, &dSelPos, &dOutK, &dOutC})
+    for (DevBuf *b : {&dReads, &dHist, &dK, &dV, &dK2, &dV2, &dScr, &dFlags, &dPos, &dRun, &dSel, &dSelPos, &dOutK, &dOutC})
       b->release();
   };
-  int rc = OIC_OK;
+  int  rc   = OIC_OK;
   auto step = [&](cudaError_t e) {
     if (e != cudaSuccess && !rc) rc = fail(ctx, OIC_ERR_CUDA, "k-mer count: %s", cudaGetErrorString(e));
     return rc == OIC_OK;
   };
-  const size_t nr = reads.size();
-  if (step(dReads.ensure(nr * 4)) && step(dFlat.ensure((nr + 1) * 8)) && step(dK.ensure(n * 8)) && step(dV.ensure(n * 4)) &&
-      step(dK2.ensure(n * 8)) && step(dV2.ensure(n * 4)) &&
-      step(dScr.ensure(std::max(radix_sort_scratch(n), scan_u32_scratch(n)) + 256)) && step(dFlags.ensure(n * 4)) &&
-      step(dPos.ensure(n * 4)) && step(cudaMemcpyAsync(dReads.p, reads.data(), nr * 4, cudaMemcpyHostToDevice, ctx->st)) &&
-      step(cudaMemcpyAsync(dFlat.p, flat.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, ctx->st)) &&
+
+  // Key-space parts: the top 12 bits of the 2K-bit canonical key.  A pass sorts the
+  // windows of consecutive parts, at most passMax of them (sized from the free memory:
+  // about 48 bytes per window; OIC_KMER_PASS_WINDOWS lowers it for testing).
+  const int   P     = canon_parts();
+  const int   shift = std::max(0, 2 * K - 12);
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  uint64_t passMax = std::min<uint64_t>(0xfffffffeull, (uint64_t)(0.6 * (double)freeB / 48.0));
+  if (const char *e = getenv("OIC_KMER_PASS_WINDOWS")) passMax = std::max<uint64_t>(1, strtoull(e, nullptr, 10));
+  std::vector<unsigned long long> hist(P, 0);
+  unsigned long long              nInvalid = 0;
+  if (step(dReads.ensure((size_t)nr * 4)) && step(dHist.ensure((size_t)P * 8)) &&
+      step(cudaMemcpyAsync(dReads.p, reads.data(), (size_t)nr * 4, cudaMemcpyHostToDevice, ctx->st)) &&
+      step(cudaMemsetAsync(dHist.p, 0, (size_t)P * 8, ctx->st)) &&
       step(cudaMemsetAsync(ctr64(ctx) + kCellsSnap, 0, 8, ctx->st))) {
-    launch_canon_emit(ctx->R, dReads.as<uint32_t>(), (uint32_t)nr, dFlat.as<u64>(), K, dK.as<u64>(), dV.as<uint32_t>(),
+    launch_canon_hist(ctx->R, dReads.as<uint32_t>(), nr, K, shift, dHist.as<unsigned long long>(),
                       ctr64(ctx) + kCellsSnap, ctx->st);
-    step(radix_sort_u64_u32(dK.as<u64>(), dV.as<uint32_t>(), dK2.as<u64>(), dV2.as<uint32_t>(), n, 2 * K + 1, dScr.p,
-                            ctx->st));
+    if (step(cudaMemcpyAsync(hist.data(), dHist.p, (size_t)P * 8, cudaMemcpyDeviceToHost, ctx->st)) &&
+        step(cudaMemcpyAsync(&nInvalid, ctr64(ctx) + kCellsSnap, 8, cudaMemcpyDeviceToHost, ctx->st)))
+      rc = sync_check(ctx, "k-mer histogram");
   }
-  unsigned long long nInvalid = 0;
-  if (!rc && step(cudaMemcpyAsync(&nInvalid, ctr64(ctx) + kCellsSnap, 8, cudaMemcpyDeviceToHost, ctx->st)))
-    rc = sync_check(ctx, "k-mer sort");
-  const uint64_t nValid = n - nInvalid;   // invalid keys sort last
-  uint32_t       nRuns = 0, nSel = 0;
-  if (!rc && nValid) {
-    launch_run_starts(dK.as<u64>(), nValid, dFlags.as<uint32_t>(), ctx->st);
-    if (step(scan_u32(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nValid, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) &&
-        step(cudaMemcpyAsync(&nRuns, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)))
-      rc = sync_check(ctx, "k-mer runs");
-    if (!rc && step(dRun.ensure((size_t)nRuns * 8 + 8)) && step(dSel.ensure((size_t)nRuns * 4 + 4)) &&
-        step(dSelPos.ensure((size_t)nRuns * 4 + 4))) {
-      launch_run_index(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nValid, dRun.as<u64>(), ctx->st);
-      launch_run_select(dRun.as<u64>(), nRuns, nValid, minCount, dSel.as<uint32_t>(), ctx->st);
-      if (step(scan_u32(dSel.as<uint32_t>(), dSelPos.as<uint32_t>(), nRuns, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) &&
-          step(cudaMemcpyAsync(&nSel, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)))
-        rc = sync_check(ctx, "k-mer selection");
-    }
+  // Passes: consecutive parts while their windows fit.
+  std::vector<std::pair<uint32_t, uint32_t>> passes;
+  uint64_t                                   biggest = 0;
+  for (int p = 0; !rc && p < P;) {
+    uint64_t w = 0;
+    int      q = p;
+    while (q < P && (q == p || w + hist[q] <= passMax)) w += hist[q++];
+    if (w > 0xfffffffeull)
+      rc = fail(ctx, OIC_ERR_OVERFLOW, "one k-mer key range holds more than 2^32-2 windows");
+    if (w) passes.push_back({(uint32_t)p, (uint32_t)q});
+    biggest = std::max(biggest, w);
+    p       = q;
   }
-  if (!rc && nSel) {
-    *nKmers = nSel;
-    if (nSel > maxKmers) rc = fail(ctx, OIC_ERR_OVERFLOW, "%u k-mers found, room for %lu", nSel, (unsigned long)maxKmers);
-    else if (step(dOutK.ensure((size_t)nSel * 8)) && step(dOutC.ensure((size_t)nSel * 4))) {
-      launch_run_compact(dK.as<u64>(), dRun.as<u64>(), nRuns, nValid, dSel.as<uint32_t>(), dSelPos.as<uint32_t>(),
-                         dOutK.as<u64>(), dOutC.as<uint32_t>(), ctx->st);
-      std::vector<uint64_t> keys(nSel);
-      if (step(cudaMemcpyAsync(keys.data(), dOutK.p, (size_t)nSel * 8, cudaMemcpyDeviceToHost, ctx->st)) &&
-          step(cudaMemcpyAsync(counts, dOutC.p, (size_t)nSel * 4, cudaMemcpyDeviceToHost, ctx->st)) &&
-          !(rc = sync_check(ctx, "k-mer output"))) {
-        static const char acgt[4] = {'A', 'C', 'G', 'T'};
-        for (uint32_t i = 0; i < nSel; i++)
-          for (int b = 0; b < K; b++) kmers[(size_t)i * K + b] = acgt[(keys[i] >> (2 * b)) & 3];
-      }
-    }
+  const uint64_t m = biggest;
+  std::vector<uint64_t> outKeys;
+  std::vector<uint32_t> outCounts;
+  if (!rc && m &&
+      !(step(dK.ensure(m * 8)) && step(dV.ensure(m * 4)) && step(dK2.ensure(m * 8)) && step(dV2.ensure(m * 4)) &&
+        step(dScr.ensure(std::max(radix_sort_scratch(m), scan_u32_scratch(m)) + 256)) && step(dFlags.ensure(m * 4)) &&
+        step(dPos.ensure(m * 4))))
+    rc = rc ? rc : OIC_ERR_NOMEM;
+  for (size_t pi = 0; !rc && pi < passes.size(); pi++) {
+    unsigned long long nPass = 0;
+    if (!step(cudaMemsetAsync(ctr64(ctx) + kCellsSnap, 0, 8, ctx->st))) break;
+    launch_canon_emit_part(ctx->R, dReads.as<uint32_t>(), nr, K, shift, passes[pi].first, passes[pi].second,
+                           dK.as<u64>(), dV.as<uint32_t>(), ctr64(ctx) + kCellsSnap, ctx->st);
+    if (!step(cudaMemcpyAsync(&nPass, ctr64(ctx) + kCellsSnap, 8, cudaMemcpyDeviceToHost, ctx->st)) ||
+        (rc = sync_check(ctx, "k-mer emission")))
+      break;
+    if (!nPass) continue;
+    if (!step(radix_sort_u64_u32(dK.as<u64>(), dV.as<uint32_t>(), dK2.as<u64>(), dV2.as<uint32_t>(), nPass, 2 * K,
+                                 dScr.p, ctx->st)))
+      break;
+    uint32_t nRuns = 0, nSel = 0;
+    launch_run_starts(dK.as<u64>(), nPass, dFlags.as<uint32_t>(), ctx->st);
+    if (!step(scan_u32(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nPass, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) ||
+        !step(cudaMemcpyAsync(&nRuns, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)) ||
+        (rc = sync_check(ctx, "k-mer runs")))
+      break;
+    if (!step(dRun.ensure((size_t)nRuns * 8 + 8)) || !step(dSel.ensure((size_t)nRuns * 4 + 4)) ||
+        !step(dSelPos.ensure((size_t)nRuns * 4 + 4)))
+      break;
+    launch_run_index(dFlags.as<uint32_t>(), dPos.as<uint32_t>(), nPass, dRun.as<u64>(), ctx->st);
+    launch_run_select(dRun.as<u64>(), nRuns, nPass, minCount, dSel.as<uint32_t>(), ctx->st);
+    if (!step(scan_u32(dSel.as<uint32_t>(), dSelPos.as<uint32_t>(), nRuns, ctr32(ctx) + cRecTotal, dScr.p, ctx->st)) ||
+        !step(cudaMemcpyAsync(&nSel, ctr32(ctx) + cRecTotal, 4, cudaMemcpyDeviceToHost, ctx->st)) ||
+        (rc = sync_check(ctx, "k-mer selection")))
+      break;
+    if (!nSel) continue;
+    if (!step(dOutK.ensure((size_t)nSel * 8)) || !step(dOutC.ensure((size_t)nSel * 4))) break;
+    launch_run_compact(dK.as<u64>(), dRun.as<u64>(), nRuns, nPass, dSel.as<uint32_t>(), dSelPos.as<uint32_t>(),
+                       dOutK.as<u64>(), dOutC.as<uint32_t>(), ctx->st);
+    const size_t at = outKeys.size();
+    outKeys.resize(at + nSel);
+    outCounts.resize(at + nSel);
+    if (!step(cudaMemcpyAsync(outKeys.data() + at, dOutK.p, (size_t)nSel * 8, cudaMemcpyDeviceToHost, ctx->st)) ||
+        !step(cudaMemcpyAsync(outCounts.data() + at, dOutC.p, (size_t)nSel * 4, cudaMemcpyDeviceToHost, ctx->st)) ||
+        (rc = sync_check(ctx, "k-mer output")))
+      break;
   }
   release();
-  return rc;
+  if (rc) return rc;
+  // Parts ascend with the key, and every pass's output ascends: the concatenation does.
+  *nKmers = outKeys.size();
+  if (outKeys.size() > maxKmers)
+    return fail(ctx, OIC_ERR_OVERFLOW, "%zu k-mers found, room for %lu", outKeys.size(), (unsigned long)maxKmers);
+  static const char acgt[4] = {'A', 'C', 'G', 'T'};
+  for (size_t i = 0; i < outKeys.size(); i++) {
+    for (int b = 0; b < K; b++) kmers[i * K + b] = acgt[(outKeys[i] >> (2 * b)) & 3];
+    counts[i] = outCounts[i];
+  }
+  if (verbose())
+    fprintf(stderr, "oic: k-mer count: %lu windows (%llu with N) in %zu passes\n", (unsigned long)n, nInvalid,
+            passes.size());
+  return OIC_OK;
 }
 
 int oic_set_tuning(oic_ctx *ctx, const oic_tuning *t) {

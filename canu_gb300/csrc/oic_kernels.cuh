@@ -175,8 +175,13 @@ void launch_list_keys(const PairRec *pairs, const u32 *list, u32 n, unsigned lon
                       cudaStream_t st);
 
 // ---------------- frequent k-mers (oic_kmers.cu) ----------------
-void launch_canon_emit(ReadsDev R, const u32 *reads, u32 nReads, const u64 *flatStart, int K, u64 *keys, u32 *vals,
+// Partitioned count: hist[part] (canon_parts() parts, part = key >> shift) of the valid
+// windows of `reads`, then the windows of parts [p0, p1) appended at *counter.
+int  canon_parts();
+void launch_canon_hist(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, unsigned long long *hist,
                        unsigned long long *nInvalid, cudaStream_t st);
+void launch_canon_emit_part(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, u32 p0, u32 p1, u64 *keys,
+                            u32 *vals, unsigned long long *counter, cudaStream_t st);
 void launch_run_starts(const u64 *keys, u64 nValid, u32 *flags, cudaStream_t st);
 void launch_run_index(const u32 *flags, const u32 *pos, u64 nValid, u64 *runStart, cudaStream_t st);
 void launch_run_select(const u64 *runStart, u32 nRuns, u64 nValid, u32 minCount, u32 *sel, cudaStream_t st);

@@ -8,7 +8,10 @@
 // strands folded into one canonical key: the smaller of the window's key and its
 // reverse complement's, in the 2-bit encoding of oic_common.cuh) is emitted, radix
 // sorted, and the runs of equal keys are counted; runs of at least minCount are kept.
-// Windows holding an N are skipped.
+// Windows holding an N are skipped.  Read sets with more windows than one sort holds are
+// counted in passes over ranges of the key space: a histogram of the keys' top bits
+// (4096 parts) splits the key space into ranges of at most a pass's windows, and each
+// pass emits only the windows whose key falls in its range.
 #include "oic_kernels.cuh"
 #include "oic_prims.cuh"
 
@@ -16,36 +19,91 @@ namespace oic {
 
 namespace {
 
-// Block per read: canonical key of every window, or `invalid` (2^2K, sorts last) for a
-// window with an N.  nInvalid counts those.
-__global__ void canon_emit_kernel(ReadsDev R, const u32 *reads, u32 nReads, const u64 *flatStart, int K, u64 *keys,
-                                  u32 *vals, unsigned long long *nInvalid) {
+// Canonical key of window o of read r (base offset g0 of its words), or `invalid` for a
+// window with an N.
+__device__ __forceinline__ u64 canon_key(const ReadsDev &R, i64 g0, u32 L, u32 o, int K, bool hn, u64 kmask,
+                                         u64 invalid) {
+  const u64 fk = load_win(R.fwd, g0 + o) & kmask;
+  const u64 rk = load_win(R.rc, g0 + (i64)(L - K - o)) & kmask;
+  if (hn && (load_win(R.nfwd, g0 + o) & kmask)) return invalid;
+  return fk < rk ? fk : rk;
+}
+
+// hist[key >> shift] for every valid window (kParts parts), via a block histogram.
+constexpr int kParts = 4096;
+__global__ void canon_hist_kernel(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, unsigned long long *hist,
+                                  unsigned long long *nInvalid) {
+  __shared__ unsigned int h[kParts];
+  for (int i = threadIdx.x; i < kParts; i += blockDim.x) h[i] = 0;
+  __syncthreads();
   const u64 kmask   = (K >= 32) ? ~0ull : ((1ull << (2 * K)) - 1);
   const u64 invalid = 1ull << (2 * K);
   unsigned long long bad = 0;
   for (u32 s = blockIdx.x; s < nReads; s += gridDim.x) {
-    const u32 r  = reads[s];
-    const u32 L  = R.len[r];
+    const u32 r = reads[s];
+    const u32 L = R.len[r];
     if (L < (u32)K) continue;
-    const u32 nk = L - K + 1;
-    const i64 g0 = (i64)R.wordOff[r] * 32;
+    const i64  g0 = (i64)R.wordOff[r] * 32;
     const bool hn = R.hasN[r] != 0;
-    const u64 f0 = flatStart[s];
-    for (u32 o = threadIdx.x; o < nk; o += blockDim.x) {
-      // The reverse complement of forward window o is the reverse-strand window at
-      // offset L - K - o.
-      const u64 fk = load_win(R.fwd, g0 + o) & kmask;
-      const u64 rk = load_win(R.rc, g0 + (i64)(L - K - o)) & kmask;
-      u64 key      = fk < rk ? fk : rk;
-      if (hn && (load_win(R.nfwd, g0 + o) & kmask)) {
-        key = invalid;
-        bad++;
-      }
-      keys[f0 + o] = key;
-      vals[f0 + o] = 0;
+    for (u32 o = threadIdx.x; o < L - K + 1; o += blockDim.x) {
+      const u64 key = canon_key(R, g0, L, o, K, hn, kmask, invalid);
+      if (key == invalid) bad++;
+      else atomicAdd(&h[key >> shift], 1u);
+    }
+    // Flush before a block's counters could wrap (a read has < 2^21 windows).
+    if (((s / gridDim.x) & 1023) == 1023) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < kParts; i += blockDim.x)
+        if (h[i]) {
+          atomicAdd(&hist[i], (unsigned long long)h[i]);
+          h[i] = 0;
+        }
+      __syncthreads();
     }
   }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kParts; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
   if (bad) atomicAdd(nInvalid, bad);
+}
+
+// The valid windows whose key's part lies in [p0, p1), appended at counter positions
+// (one atomic per warp and step).
+__global__ void canon_emit_part_kernel(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, u32 p0, u32 p1,
+                                       u64 *keys, u32 *vals, unsigned long long *counter) {
+  const u64 kmask   = (K >= 32) ? ~0ull : ((1ull << (2 * K)) - 1);
+  const u64 invalid = 1ull << (2 * K);
+  const int lane    = threadIdx.x & 31;
+  for (u32 s = blockIdx.x; s < nReads; s += gridDim.x) {
+    const u32 r = reads[s];
+    const u32 L = R.len[r];
+    if (L < (u32)K) continue;   // uniform across the block
+    const i64  g0 = (i64)R.wordOff[r] * 32;
+    const bool hn = R.hasN[r] != 0;
+    const u32  nk = L - K + 1;
+    for (u32 o0 = threadIdx.x & ~31u; o0 < nk; o0 += blockDim.x) {
+      const u32 o = o0 + lane;
+      u64  key  = invalid;
+      bool take = false;
+      if (o < nk) {
+        key = canon_key(R, g0, L, o, K, hn, kmask, invalid);
+        if (key != invalid) {
+          const u32 part = (u32)(key >> shift);
+          take           = part >= p0 && part < p1;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, take);
+      if (!m) continue;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(counter, (unsigned long long)__popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (take) {
+        const u64 at = base + __popc(m & ((1u << lane) - 1));
+        keys[at] = key;
+        vals[at] = 0;
+      }
+    }
+  }
 }
 
 // flags[i] = 1 where a run of equal valid keys starts (i < nValid).
@@ -88,11 +146,20 @@ unsigned grid_for(u64 n, unsigned per = 256) {
 
 }  // namespace
 
-void launch_canon_emit(ReadsDev R, const u32 *reads, u32 nReads, const u64 *flatStart, int K, u64 *keys, u32 *vals,
+int canon_parts() { return kParts; }
+
+void launch_canon_hist(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, unsigned long long *hist,
                        unsigned long long *nInvalid, cudaStream_t st) {
   if (nReads == 0) return;
-  canon_emit_kernel<<<nReads < 65535u * 4 ? nReads : 65535u * 4, 256, 0, st>>>(R, reads, nReads, flatStart, K, keys,
-                                                                             vals, nInvalid);
+  canon_hist_kernel<<<nReads < 152u * 8 ? nReads : 152u * 8, 256, 0, st>>>(R, reads, nReads, K, shift, hist, nInvalid);
+  g_launches++;
+}
+
+void launch_canon_emit_part(ReadsDev R, const u32 *reads, u32 nReads, int K, int shift, u32 p0, u32 p1, u64 *keys,
+                            u32 *vals, unsigned long long *counter, cudaStream_t st) {
+  if (nReads == 0) return;
+  canon_emit_part_kernel<<<nReads < 65535u * 4 ? nReads : 65535u * 4, 256, 0, st>>>(R, reads, nReads, K, shift, p0, p1,
+                                                                                   keys, vals, counter);
   g_launches++;
 }
 

@@ -305,7 +305,9 @@ int oic_autotune(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID, double *rep
  * are skipped.  Writes up to maxKmers k-mers with count >= minCount -- kmerLen bases
  * each (ACGT), concatenated -- and their counts (saturating at 2^32-1), in ascending
  * order of the canonical 2-bit key; *nKmers gets the number found (larger than
- * maxKmers: OIC_ERR_OVERFLOW, call again with room).  At most 2^32-2 windows. */
+ * maxKmers: OIC_ERR_OVERFLOW, call again with room).  Read sets with more windows than
+ * one sort holds (2^32 - 2, or what the free device memory takes) are counted in
+ * passes over ranges of the canonical key space. */
 int oic_count_kmers(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t minCount, char *kmers, uint32_t *counts,
                     uint64_t maxKmers, uint64_t *nKmers);
 

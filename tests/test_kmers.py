@@ -54,6 +54,24 @@ def test_gpu_count_matches_oracle(case, min_count, built, golden_inputs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pass_windows", [20000, 60000])
+def test_gpu_count_in_key_space_passes_matches_oracle(pass_windows, built, golden_inputs, monkeypatch):
+    """Read sets beyond one sort (2^32 windows, e.g. 8 Gbp of reads) are counted in
+    passes over ranges of the canonical key space; forcing small passes here must give
+    the same k-mers and counts, in the same ascending key order."""
+    db = golden_inputs["default"]["db"]
+    lib, ln, off, bases = oic.read_seqdb(db)
+    reads = [bytes(bases[o:o + l]) for o, l in zip(off.tolist(), ln.tolist())][:400]
+    monkeypatch.setenv("OIC_KMER_PASS_WINDOWS", str(pass_windows))
+    with oic.Overlapper(oic.default_params(kmerLen=22)) as ov:
+        ov.set_reads_seqdb(db)
+        strs, cnt = ov.count_kmers(1, len(reads), 1)
+    ref_s, ref_c = ko.frequent(reads, 22, 1)
+    assert int((ln[:400].astype(np.int64) - 21).sum()) > 5 * pass_windows     # several passes
+    assert strs == ref_s and np.array_equal(cnt, ref_c)
+
+
+@pytest.mark.gpu
 def test_skip_file_tool_writes_a_list_overlapincore_reads(built, golden_inputs, tmp_path):
     g = golden_inputs["repeats_noskip"] if "repeats_noskip" in golden_inputs else golden_inputs["default"]
     out = str(tmp_path / "ms22.dump")
