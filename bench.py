@@ -471,9 +471,9 @@ def main():
     alg_bytes = pairs * (32 + 72 + 4 + 2 * mean_len / 4) + nodes * 16
     achieved = alg_bytes / (ms_align / 1000.0) / 1e9
     # DRAM bytes per DP cell of the one-warp DP kernel, from one ncu capture of a 1/50
-    # scale c2 launch (10.73 GB read + 22.65 GB written for 6.598 G cells; the figures and
+    # scale c2 launch (10.54 GB read + 22.94 GB written for 6.598 G cells; the figures and
     # the command are in profiles/align_kernel_c2_scale0.02_ncu.md), scaled to this job.
-    traffic = 5.059 * cells
+    traffic = 5.074 * cells
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
     int_ops = 6 * cells + slides / 16.0
@@ -488,10 +488,11 @@ def main():
     ms_seed = statistics.mean(r[0]["msSeed"] for r in res)
     sort_passes = (2 * K + 1 + 7) // 8
 
-    def stage_roof(nbytes, ms, basis):
+    def stage_roof(nbytes, ms, basis, traffic=None, traffic_basis=None):
         ach = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else None
         return {"achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": ach / peaks["hbm_gbs"] if ach else None, "bytes": nbytes, "ms": ms, "basis": basis}
+                "frac": ach / peaks["hbm_gbs"] if ach else None, "bytes": nbytes, "ms": ms, "basis": basis,
+                "traffic": traffic, "traffic_basis": traffic_basis}
     hash_bytes = 0.25 * n_bases + 12 * n_kmers
     seed_bytes = 2 * n_bases * (0.25 + 32) + 12 * float(st0["seeds"])
     line = {
@@ -520,8 +521,14 @@ def main():
                                           "INT32 lanes x median SM clock"},
                      "hash": stage_roof(hash_bytes, ms_hash, "0.25 B/base + 12 B/k-mer (sort passes excluded)"),
                      "hash_with_sort": stage_roof(hash_bytes + sort_passes * 24 * n_kmers, ms_hash,
-                                                  f"as hash + {sort_passes} radix passes x 24 B/k-mer"),
-                     "seed": stage_roof(seed_bytes, ms_seed, "2 strands x (0.25 B/base + 32 B/lookup) + 12 B/seed")},
+                                                  f"as hash + {sort_passes} radix passes x 24 B/k-mer",
+                                                  sort_passes * 24.1 * n_kmers,
+                                                  "radix passes only: ncu 24.1 B DRAM per key and pass "
+                                                  "(profiles/radix_downsweep_c2_scale0.25_ncu.md)"),
+                     "seed": stage_roof(seed_bytes, ms_seed, "2 strands x (0.25 B/base + 32 B/lookup) + 12 B/seed",
+                                        54.9 * float(st0["seeds"]),
+                                        "ncu 54.9 B DRAM per seed of a 1/4-scale c2 launch x this job's seeds "
+                                        "(profiles/seed_kernel_c2_scale0.25_ncu.md)")},
         "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in res)),
         "clocks": clk,
     }
