@@ -419,9 +419,13 @@ def main():
     # The learned candidate filter on the same reads (trained on other seeds).
     filt = None
     fpath = os.path.join(ROOT, "canu_gb300", "filter_c2.npz")
-    if a.workload == "c2" and os.path.exists(fpath) and not a.no_filter:
+    fmeta = None
+    if os.path.exists(fpath) and not a.no_filter:
         from canu_gb300 import filter_train
         fprm, fthr, ffull, fmeta = filter_train.load(fpath)
+        if fmeta["domain"] != filter_train.training_domain(a.workload):
+            fmeta = None        # the network serves only the parameters it was trained under
+    if fmeta is not None:
         ov.set_filter(fprm, fthr, ffull, fmeta.get("budget", 1), domain=fmeta["domain"])
         fres, _, frec = timed(False)
         ov.set_filter(None, 0.0)
@@ -439,8 +443,8 @@ def main():
                 "ms_filter": fst["msFilter"], "ms_align": fst["msAlign"],
                 "thresholds": {"drop_below_p": fthr, "budget_tier_below_p": ffull,
                                "extension_budget": fmeta.get("budget", 1)},
-                "trained_on": f"c2 seeds {fmeta.get('train_seeds')}; this read set is seed "
-                              f"{workloads.WORKLOADS[a.workload]['synth']['seed']} (held out)",
+                "trained_on": f"c2 seeds {fmeta.get('train_seeds')}; this read set is {a.workload} seed "
+                              f"{workloads.WORKLOADS[a.workload]['synth']['seed']} (not seen in training)",
                 "gpu_launches": int(sum(r[0]["kernelLaunches"] for r in fres))}
     # The CPU baseline (rank 0, one GPU): the oracle on a spread sample of ref reads, and
     # the GPU's records for the same ref reads compared with the oracle's.
