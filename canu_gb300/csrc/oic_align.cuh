@@ -255,8 +255,9 @@ __device__ __forceinline__ void group_bar(int id, int nThr) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(nThr) : "memory");
 }
 
-// The row loop by one warp.  Row 0 (value r0) is in prev[2].
-template <int STEP>
+// The row loop by one warp.  Row 0 (value r0) is in prev[2].  FIRST16: slides start
+// with a 16-base compare (see slide()).
+template <int STEP, bool FIRST16>
 __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, int a0, int m, const SeqView &Tref,
                                              int t0, int n, int errorLimit) {
   const SeqView A = Aref, T = Tref;   // in registers for the slides
@@ -309,7 +310,7 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, int
       if (pm > row) row = pm;
       if (1 + pp > row) row = 1 + pp;
       const int room = min(m - row, n - row - d);
-      if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, slides);
+      if (room > 0) row += slide<STEP, FIRST16>(A, a0, T, t0, row, d, room, slides);
       cv[d] = row;
       if ((row == m || row + d == n) && d < myEnd) myEnd = d;
       // pruneAlign (prefixEditDistance.H:249-258): extra = max(d, 0) on both band edges
@@ -525,7 +526,7 @@ static __device__ __noinline__ void group_worker(GroupShared &gs, const WarpScra
 // view A, T likewise.  The row loop runs on this warp, or on the whole CTA when w.gs is
 // set (warp 0 of a group CTA); the rest runs on this warp.  Returns the error count;
 // the outputs are warp-uniform.  On a capacity overflow sets w.err and returns 0.
-template <int STEP, bool GROUP>
+template <int STEP, bool GROUP, bool FIRST16 = false>
 static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, int a0, int m, const SeqView &T, int t0, int n,
                               int errorLimit, int &aEnd, int &tEnd, int &leftover, bool &toEnd) {
   const int lane = threadIdx.x & 31;
@@ -571,7 +572,7 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
     const GroupJob j = w.gs->job;
     o = group_rows_any(j, w.sc, w.cap, w.eml, lane, w.gThreads, w.gs->red, w.slides);
   } else {
-    o = warp_rows<STEP>(w, A, a0, m, T, t0, n, errorLimit);
+    o = warp_rows<STEP, FIRST16>(w, A, a0, m, T, t0, n, errorLimit);
   }
   w.cells += o.cells;
   w.rows += o.rows;
@@ -666,7 +667,7 @@ enum { kNone = 0, kLeftBranch = 1, kRightBranch = 2, kDovetail = 3 };
 
 // Extend_Alignment (prefixEditDistance-extend.C:36-183), one warp.  The merged delta
 // ends up in sc.deltaL[0 .. leftLen).  Outputs are warp-uniform.
-template <bool GROUP>
+template <bool GROUP, bool FIRST16 = false>
 static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int sLen, const SeqView &T, int tLen, int mStart,
                            int mOffset, int mLen, int &sLo, int &sHi, int &tLo, int &tHi, int &errors) {
   const int lane = threadIdx.x & 31;
@@ -685,12 +686,12 @@ static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int 
     sHi = tHi = 0;
     rToEnd    = true;
   } else if (sRightLen <= tRightLen) {
-    rightErrors = warp_prefix_dp<+1, GROUP>(w, S, sRightBegin, sRightLen, T, tRightBegin, tRightLen, errorLimit, sHi, tHi,
+    rightErrors = warp_prefix_dp<+1, GROUP, FIRST16>(w, S, sRightBegin, sRightLen, T, tRightBegin, tRightLen, errorLimit, sHi, tHi,
                                      leftover, rToEnd);
     if (w.err) return kNone;
     for (int i = lane; i < w.rightLen; i += 32) w.sc.deltaR[i] = -w.sc.deltaR[i];
   } else {
-    rightErrors = warp_prefix_dp<+1, GROUP>(w, T, tRightBegin, tRightLen, S, sRightBegin, sRightLen, errorLimit, tHi, sHi,
+    rightErrors = warp_prefix_dp<+1, GROUP, FIRST16>(w, T, tRightBegin, tRightLen, S, sRightBegin, sRightLen, errorLimit, tHi, sHi,
                                      leftover, rToEnd);
     if (w.err) return kNone;
   }
@@ -703,11 +704,11 @@ static __device__ __noinline__ int warp_extend(WarpDP &w, const SeqView &S, int 
     sLo = tLo = 0;
     lToEnd    = true;
   } else if (sRightBegin <= tRightBegin) {
-    leftErrors = warp_prefix_dp<-1, GROUP>(w, S, sLeftBegin, sLeftBegin + 1, T, tLeftBegin, tLeftBegin + 1,
+    leftErrors = warp_prefix_dp<-1, GROUP, FIRST16>(w, S, sLeftBegin, sLeftBegin + 1, T, tLeftBegin, tLeftBegin + 1,
                                     errorLimit - rightErrors, sLo, tLo, leftover, lToEnd);
     if (w.err) return kNone;
   } else {
-    leftErrors = warp_prefix_dp<-1, GROUP>(w, T, tLeftBegin, tLeftBegin + 1, S, sLeftBegin, sLeftBegin + 1,
+    leftErrors = warp_prefix_dp<-1, GROUP, FIRST16>(w, T, tLeftBegin, tLeftBegin + 1, S, sLeftBegin, sLeftBegin + 1,
                                     errorLimit - rightErrors, tLo, sLo, leftover, lToEnd);
     if (w.err) return kNone;
     for (int i = lane; i < w.leftLen; i += 32) w.sc.deltaL[i] = -w.sc.deltaL[i];

@@ -119,16 +119,56 @@ __device__ __forceinline__ int match_run32(const SeqView &A, int a, const SeqVie
   return mm ? (__ffsll((long long)mm) - 1) >> 1 : 32;
 }
 
-// Bases that agree from A[step*row] / T[step*(row+d)] on, capped at `lim`.
+// 16 bases starting at base g of one read, from the strand viewed as 32-bit words (base
+// i in bits 2*(i%16) of word i/16 on a little-endian device): one funnel shift.  The
+// guard word before a read keeps g >= -32 in bounds.
+__device__ __forceinline__ u32 load_win16(const u64 *w, int g) {
+  const u32 *w32 = reinterpret_cast<const u32 *>(w);
+  const int  wi  = g >> 4;
+  return __funnelshift_r(__ldg(w32 + wi), __ldg(w32 + wi + 1), (g & 15) * 2);
+}
+
+// Number of leading bases (0..16) that agree between A (from a) and T (from t), N
+// matching anything: a cheaper first step for slides that are mostly short.
 template <int STEP>
+__device__ __forceinline__ int match_run16(const SeqView &A, int a, const SeqView &T, int t) {
+  u32 wa, wt;
+  if (STEP > 0) {
+    wa = load_win16(A.w, a);
+    wt = load_win16(T.w, t);
+  } else {
+    wa = __brev(load_win16(A.w, a - 15));
+    wt = __brev(load_win16(T.w, t - 15));
+  }
+  const u32 x  = wa ^ wt;
+  u32       mm = (x | (x >> 1)) & 0x55555555u;
+  if (mm && (A.nm || T.nm)) {
+    u32 n = 0;
+    if (A.nm) n |= (STEP > 0) ? load_win16(A.nm, a) : __brev(load_win16(A.nm, a - 15));
+    if (T.nm) n |= (STEP > 0) ? load_win16(T.nm, t) : __brev(load_win16(T.nm, t - 15));
+    mm &= ~n;
+  }
+  return mm ? (__ffs((int)mm) - 1) >> 1 : 16;
+}
+
+// Bases that agree from A[step*row] / T[step*(row+d)] on, capped at `lim` (> 0).  The
+// first step compares 32 bases, or 16 when FIRST16 (cheaper when most slides end
+// within a few bases, as at higher error rates); the rest go 32 at a time.
+template <int STEP, bool FIRST16 = false>
 __device__ __forceinline__ int slide(const SeqView &A, int a0, const SeqView &T, int t0, int row, int d, int lim,
                                      unsigned long long &slides) {
-  int run = 0;
-  while (run < lim) {
-    int r = match_run32<STEP>(A, a0 + STEP * (row + run), T, t0 + STEP * (row + d + run));
-    run += r;
-    if (r < 32) break;
+  int  run  = 0;
+  bool more = true;
+  if (FIRST16) {
+    run  = match_run16<STEP>(A, a0 + STEP * row, T, t0 + STEP * (row + d));
+    more = run == 16;
   }
+  if (more)
+    while (run < lim) {
+      int r = match_run32<STEP>(A, a0 + STEP * (row + run), T, t0 + STEP * (row + d + run));
+      run += r;
+      if (r < 32) break;
+    }
   if (run > lim) run = lim;
   slides += (unsigned long long)run;
   return run;
