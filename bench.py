@@ -59,6 +59,14 @@ WORKLOAD_TEXT = {
            "--hashdatalen 2e9 (4 hash blocks); frequent-k-mer skip list"),
 }
 
+def workload_text(a):
+    """The workload's description; without its skip list, said so."""
+    t = WORKLOAD_TEXT.get(a.workload, a.workload)
+    if a.no_skip_list:
+        t = t.split("; frequent-k-mer skip list")[0] + "; no frequent-k-mer skip list (the configuration as written)"
+    return t
+
+
 # Nominal INT32 lanes per SM (Blackwell: 128 unified FP32/INT32 lanes).
 INT_LANES_PER_SM = 128
 
@@ -318,7 +326,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-filter", action="store_true", help="skip the learned-filter leg")
+    ap.add_argument("--no-skip-list", action="store_true",
+                    help="run the workload without its frequent-k-mer skip list (c2 / c5 as their configurations "
+                         "are written); the learned filter, trained with the list, is left out")
     a = ap.parse_args()
+    if a.no_skip_list:
+        a.no_filter = True
     ws, rank, local = dist()
     cores = os.cpu_count() or 1
 
@@ -336,6 +349,7 @@ def main():
         if rank != 0:
             return 0
         db, skip = workloads.generate(a.workload, a.data_dir, a.scale)
+        skip = None if a.no_skip_list else skip
         cpu = CpuPath(a.workload, db, skip, cores)
         vals, samples = [], []
         chunks = spread_chunks(cpu.nReads)
@@ -351,7 +365,7 @@ def main():
         line = {"impl": "reference", "metric": "overlaps_per_sec", "value": v, "unit": "overlaps/s", "n_gpus": 0,
                 "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * statistics.mean(s[0] for s in samples),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-                "data": "synthetic", "config": {"workload": WORKLOAD_TEXT.get(a.workload, a.workload),
+                "data": "synthetic", "config": {"workload": workload_text(a),
                                                 "scale": a.scale, "reads": cpu.nReads},
                 "cpu_baseline": {"value": v, "unit": "overlaps/s", "cores": cores, "kind": "port",
                                  "sample": f"{nrefs} ref reads (both strands) in chunks of 16 spread over the ID "
@@ -373,6 +387,7 @@ def main():
     if ws > 1:
         td.barrier()
     db, skip = workloads.generate(a.workload, a.data_dir, a.scale)
+    skip = None if a.no_skip_list else skip
     lib_, ln, off, bases = oic.read_seqdb(db)
     nReads = len(ln)
     try:
@@ -503,7 +518,7 @@ def main():
         "metric": "overlaps_per_sec", "value": value, "unit": "overlaps/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_dev_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT.get(a.workload, a.workload), "scale": a.scale, "reads": nReads,
+        "config": {"workload": workload_text(a), "scale": a.scale, "reads": nReads,
                    "bases": int(bases.size), "overlaps_per_step": n_ov, "parallelism": f"replicas{ws}",
                    "l2": "inputs (2-bit reads, hash table, seed lists) larger than L2"},
         "dp_cells_per_sec": ws * cells / (ms_dev_max / 1000.0),

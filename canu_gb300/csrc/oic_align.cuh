@@ -241,6 +241,7 @@ struct GroupJob {
   SeqView A, T;
   int     a0, t0;
   int     m, n, errorLimit, step, u;
+  int     first16;           // slides start with the 16-base compare (slide_first16)
   int    *rowA, *rowB;       // row buffers (rowA holds row 0)
 };
 struct GroupShared {
@@ -373,7 +374,7 @@ __device__ __forceinline__ RowsOut warp_rows(WarpDP &w, const SeqView &Aref, int
 // neighbour values of row e-1 are read once for U cells and U slides are in flight.
 // Every decision is made on CTA-reduced values, so all threads take the same path and
 // meet the same barriers.
-template <int STEP, int U>
+template <int STEP, int U, bool FIRST16>
 static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpScratch &sc, const AlignCaps &cap,
                                                   const int *eml, int tid, int nThr, int (*red)[4],
                                                   unsigned long long &slides) {
@@ -422,7 +423,7 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
           if (q[k] > row) row = q[k];
           if (1 + q[k + 2] > row) row = 1 + q[k + 2];
           const int room = min(m - row, n - row - d);
-          if (room > 0) row += slide<STEP>(A, a0, T, t0, row, d, room, slides);
+          if (room > 0) row += slide<STEP, FIRST16>(A, a0, T, t0, row, d, room, slides);
           cv[d] = row;
           if ((row == m || row + d == n) && d < myEnd) myEnd = d;
           if (!(row + max(d, 0) < lim)) {
@@ -499,14 +500,18 @@ static __device__ __noinline__ RowsOut group_rows(const GroupJob &j, const WarpS
 static __device__ __forceinline__ RowsOut group_rows_any(const GroupJob &j, const WarpScratch &sc,
                                                          const AlignCaps &cap, const int *eml, int tid, int nThr,
                                                          int (*red)[4], unsigned long long &slides) {
+#define OIC_GROUP_ROWS(S, U)                                                                  \
+  return j.first16 ? group_rows<S, U, true>(j, sc, cap, eml, tid, nThr, red, slides)          \
+                   : group_rows<S, U, false>(j, sc, cap, eml, tid, nThr, red, slides)
   if (j.step > 0) {
-    if (j.u == 4) return group_rows<+1, 4>(j, sc, cap, eml, tid, nThr, red, slides);
-    if (j.u == 2) return group_rows<+1, 2>(j, sc, cap, eml, tid, nThr, red, slides);
-    return group_rows<+1, 1>(j, sc, cap, eml, tid, nThr, red, slides);
+    if (j.u == 4) OIC_GROUP_ROWS(+1, 4);
+    if (j.u == 2) OIC_GROUP_ROWS(+1, 2);
+    OIC_GROUP_ROWS(+1, 1);
   }
-  if (j.u == 4) return group_rows<-1, 4>(j, sc, cap, eml, tid, nThr, red, slides);
-  if (j.u == 2) return group_rows<-1, 2>(j, sc, cap, eml, tid, nThr, red, slides);
-  return group_rows<-1, 1>(j, sc, cap, eml, tid, nThr, red, slides);
+  if (j.u == 4) OIC_GROUP_ROWS(-1, 4);
+  if (j.u == 2) OIC_GROUP_ROWS(-1, 2);
+  OIC_GROUP_ROWS(-1, 1);
+#undef OIC_GROUP_ROWS
 }
 
 // Worker warps of a group CTA: run the row loops warp 0 posts until it posts exit.
@@ -563,6 +568,7 @@ static __device__ __noinline__ int warp_prefix_dp(WarpDP &w, const SeqView &A, i
       j.errorLimit = errorLimit;
       j.step       = STEP;
       j.u          = w.gU;
+      j.first16    = slide_first16(w.P.maxErate);
       j.rowA       = w.smA;
       j.rowB       = w.smB;
       w.gs->cmd    = kGroupRows;

@@ -151,6 +151,12 @@ __device__ __forceinline__ int match_run16(const SeqView &A, int a, const SeqVie
   return mm ? (__ffs((int)mm) - 1) >> 1 : 16;
 }
 
+// Whether the DP kernels start slides with the 16-base compare: above a 2 % error rate
+// most slides end within a few bases (measured: 11 % less one-warp DP time at 2 % read
+// error), while on low-error reads the slides along the alignment run ~100 bases and the
+// 32-base first step is cheaper (2 % more with the 16-base one at 0.5 % read error).
+__host__ __device__ inline bool slide_first16(double maxErate) { return maxErate > 0.02; }
+
 // Bases that agree from A[step*row] / T[step*(row+d)] on, capped at `lim` (> 0).  The
 // first step compares 32 bases, or 16 when FIRST16 (cheaper when most slides end
 // within a few bases, as at higher error rates); the rest go 32 at a time.

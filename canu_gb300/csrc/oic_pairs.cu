@@ -944,11 +944,8 @@ void launch_align(int, ReadsDev R, TableDev T, DevParams P, const int *eml, cons
   const int    blocks = (nWarps + kAlignWarpsSmall - 1) / kAlignWarpsSmall;
   const size_t smem   = align_smem_bytes(512);
   cap.bandW           = 512;
-  // A 16-base first slide step pays where most slides end after a few bases (error
-  // rates of a few percent; measured 11 % less DP time at 2 % read error) and costs a
-  // little on low-error reads, whose slides along the alignment run ~100 bases
-  // (measured 2 % more at 0.5 % read error): chosen by the error rate the run allows.
-  auto k = P.maxErate > 0.02 ? align_kernel<512, kAlignWarpsSmall, true> : align_kernel<512, kAlignWarpsSmall, false>;
+  auto k = slide_first16(P.maxErate) ? align_kernel<512, kAlignWarpsSmall, true>
+                                     : align_kernel<512, kAlignWarpsSmall, false>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k<<<blocks, kAlignWarpsSmall * 32, smem, st>>>(R, T, P, eml, pairs, work, nWork, workCounter, nodes, sc, cap, out);
   g_launches++;
