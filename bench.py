@@ -2,7 +2,7 @@
 """Benchmark of the GB300 overlapInCore path (one JSON line on stdout, rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload c2] [--scale 1.0]
+                    [--workload c2] [--scale 1.0] [--no-skip-list]
 
 A step is one whole overlapInCore job on the workload's read set: the hash block of
 all reads, then every read (both strands) against it -- seed lookup, per-pair match
@@ -27,6 +27,12 @@ the read generator, never the CUDA library.
 
 parity_vs_cpu  the GPU's records for the CPU baseline's sampled ref reads (same hash
          block) compared record for record with the oracle's.
+
+--no-skip-list runs a workload that has a frequent-k-mer skip list (c2, c5) without it,
+as those configurations are written.  Their tandem arrays then give k-mers with
+~10^4-10^5 occurrences, and the seeds of the reads that cross them grow with the square
+of the genome size, for this engine and for the reference alike: use it at reduced
+--scale.
 
 Multi-GPU (torchrun): every rank runs an independent replica on its own GPU (the
 stage shards into independent jobs; there is no data exchange), value = all ranks'

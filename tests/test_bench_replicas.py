@@ -51,3 +51,19 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.barrier_max(3.0, 1) == 3.0
     assert bench.replica_rate(500, 2.0, 1) == 250.0
+
+
+def test_workload_text_says_when_the_skip_list_is_left_out():
+    """A run without its skip list is labelled as the configuration as written, so its
+    line cannot be mistaken for the skip-list run; workloads without a list are unchanged."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    for wl in ("c2", "c5"):
+        with_list = bench.workload_text(argparse.Namespace(workload=wl, no_skip_list=False))
+        without = bench.workload_text(argparse.Namespace(workload=wl, no_skip_list=True))
+        assert "frequent-k-mer skip list" in with_list and "no frequent-k-mer skip list" not in with_list
+        assert without.endswith("no frequent-k-mer skip list (the configuration as written)")
+        assert without.startswith(wl + ":")
+    c1 = bench.workload_text(argparse.Namespace(workload="c1", no_skip_list=False))
+    assert c1 == bench.WORKLOAD_TEXT["c1"]
