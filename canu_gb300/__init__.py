@@ -35,7 +35,7 @@ EXPORTS = (
 # Output files (include/oic_ovfile.h): host code of the same library, no GPU needed.
 OVFILE_EXPORTS = (
     "oic_ovb_write", "oic_ovb_read", "oic_oc_path", "oic_oc_write", "oic_oc_read", "oic_merge_outputs",
-    "oic_snappy_max_length", "oic_snappy_compress", "oic_snappy_uncompress",
+    "oic_snappy_max_length", "oic_snappy_compress", "oic_snappy_uncompress", "oic_ovstore_write",
 )
 
 # Learned candidate filter (include/oic_gpu.h): feature row width, hidden width and the
@@ -142,6 +142,7 @@ def library():
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]
         lib.oic_store_sort.argtypes = [ctypes.c_int, vp, U64, U32, ctypes.c_double, vp, P(U64), vp, vp]
         lib.oic_ovb_write.argtypes = [ctypes.c_char_p, vp, U64, ctypes.c_int]
+        lib.oic_ovstore_write.argtypes = [ctypes.c_char_p, vp, U64, vp, U32, U64]
         lib.oic_ovb_read.argtypes = [ctypes.c_char_p, vp, U64, P(U64)]
         lib.oic_oc_path.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
         lib.oic_oc_write.argtypes = [ctypes.c_char_p, vp, U64, U32]
@@ -430,6 +431,16 @@ def read_ovb(path):
     out = np.zeros((n.value, 6), dtype=np.uint32)
     _file_check(lib.oic_ovb_read(os.fsencode(path), _ptr(out), n.value, ctypes.byref(n)), "read .ovb", path)
     return out
+
+
+def write_ovstore(path, records, read_lens, max_per_file=0):
+    """Write an overlap-store directory as canu's sequential store writer lays it out
+    (info, index, data files 0001-NNN, statistics) from store records ((n, 6) uint32,
+    sorted as store_sort returns them); read_lens[i] is the length of read ID i+1."""
+    r = np.ascontiguousarray(records, dtype=np.uint32).reshape(-1, 6)
+    ln = np.ascontiguousarray(read_lens, dtype=np.uint32)
+    _file_check(library().oic_ovstore_write(os.fsencode(path), _ptr(r), len(r), _ptr(ln), len(ln), int(max_per_file)),
+                "write ovStore", path)
 
 
 def oc_path(ovb_path):

@@ -10,13 +10,21 @@
 // and a 16-bit offset; 11: length 1..64 and a 32-bit offset).  The encoder works on
 // 64 KiB fragments with a 4-byte hash of recent positions, as snappy's own does, so
 // every copy stays inside its fragment and takes the 1- or 2-byte offset forms.
+//
+// The overlap-store directory (oic_ovstore_write) is laid out as canu's sequential store
+// writer lays it out (src/stores/ovStoreWriter.C:25-130): the records' data files, the
+// per-read index, the info block and the per-read overlap-score profile.
 #include <algorithm>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cmath>
 #include <string>
 #include <vector>
+
+#include <sys/stat.h>
+#include <sys/types.h>
 
 #include "oic_ovfile.h"
 
@@ -343,6 +351,154 @@ int oic_merge_outputs(const char *outOvb, const char *const *inputs, uint32_t n)
     return fail_close(g);
   if (fflush(g) != 0) return fail_close(g);
   return fclose(g) != 0 ? 1 : 0;
+}
+
+namespace {
+
+// One read's entry of the store's statistics file (oSH_ovlSco, ovStoreHistogram.H:41-44).
+constexpr int kScorePoints = 16;
+struct ScoreProfile {
+  uint16_t points[kScorePoints];
+  uint16_t scores[kScorePoints];
+};
+static_assert(sizeof(ScoreProfile) == 64, "score profile layout");
+
+// The score profile of one read from its overlaps' scores (ovStoreHistogram.C:226-259):
+// the scores sorted decreasing and sampled at up to 15 ranks spaced n/16 apart (at
+// least 1, at most 10), rounded to the nearest rank; the remaining points take the last
+// rank.  Ranks are stored in 16 bits, as the reference stores them.
+ScoreProfile score_profile(std::vector<uint16_t> &sc) {
+  std::sort(sc.begin(), sc.end(), [](uint16_t x, uint16_t y) { return x > y; });
+  const uint32_t n = (uint32_t)sc.size();
+  ScoreProfile   p;
+  double         step = (double)n / kScorePoints;
+  if (step < 1) step = 1;
+  if (step > 10) step = 10;
+  for (int i = 0; i < kScorePoints; i++) p.points[i] = (uint16_t)(n - 1);
+  double point = 0;
+  for (int i = 0; i < kScorePoints - 1 && point < n; i++, point += step) p.points[i] = (uint16_t)std::floor(point + 0.5);
+  for (int i = 0; i < kScorePoints; i++) p.scores[i] = sc[p.points[i]];
+  return p;
+}
+
+// Writes n objects to dir/name; 0 ok, 1 i/o failure.
+int save_file(const std::string &path, const void *p, size_t bytes) {
+  FILE *f = fopen(path.c_str(), "wb");
+  if (!f) return 1;
+  if (!write_all(f, p, bytes)) return fail_close(f);
+  if (fflush(f) != 0) return fail_close(f);
+  return fclose(f) != 0 ? 1 : 0;
+}
+
+}  // namespace
+
+int oic_ovstore_write(const char *dir, const uint32_t *rec, uint64_t nRecords, const uint32_t *readLen,
+                      uint32_t maxID, uint64_t maxPerFile) {
+  if (!dir || (!rec && nRecords) || (!readLen && maxID)) return 2;
+  if (maxPerFile == 0) maxPerFile = OIC_OVSTORE_MAX_PER_FILE;
+
+  // The records must be a store's: IDs within 1..maxID, in (a_iid, b_iid, data) order,
+  // with A hangs inside the A read (the score divides by the read's length).
+  for (uint64_t i = 0; i < nRecords; i++) {
+    const uint32_t *r = rec + 6 * i;
+    if (r[0] == 0 || r[0] > maxID || r[1] == 0 || r[1] > maxID) return 2;
+    if (i > 0 && std::lexicographical_compare(r, r + 6, r - 6, r)) return 2;
+    const uint64_t d0 = ((uint64_t)r[2] << 32) | r[3];
+    const uint32_t ahg5 = (uint32_t)(d0 & 0x1fffff), ahg3 = (uint32_t)((d0 >> 21) & 0x1fffff);
+    if ((uint64_t)ahg5 + ahg3 > readLen[r[0] - 1]) return 2;
+  }
+
+  if (mkdir(dir, 0755) != 0 && errno != EEXIST) return 1;
+  const std::string base(dir);
+
+  // ovStoreOfft (ovStore.H:140-170): slice, file, offset in the file, records, then
+  // the index of the read's first record in the store; 4 zero bytes of padding.
+  struct Offt {
+    uint16_t slice, piece;
+    uint32_t offset, numOlaps, pad;
+    uint64_t overlapID;
+  };
+  static_assert(sizeof(Offt) == 24, "index entry layout");
+  std::vector<Offt>         index((size_t)maxID + 1);
+  std::vector<ScoreProfile> prof((size_t)maxID + 1);
+  memset(index.data(), 0, index.size() * sizeof(Offt));
+  memset(prof.data(), 0, prof.size() * sizeof(ScoreProfile));
+
+  // The data files (ovFile(ovFileNormalWrite), ovStoreFile.C:212-238 with _isNormal):
+  // five words per record, no a_iid.  A new file starts at a read's first record once
+  // the current file holds more than maxPerFile records (ovStoreWriter.C:84-101).
+  uint32_t              piece = 0, bgnID = UINT32_MAX, endID = 0;
+  uint64_t              inPiece = 0;
+  FILE                 *f = nullptr;
+  std::vector<uint16_t> scores;
+  char                  name[32];
+  for (uint64_t i = 0; i < nRecords; i++) {
+    const uint32_t *r = rec + 6 * i;
+    const uint32_t  a = r[0];
+    if (f && inPiece > maxPerFile && endID < a) {
+      if (fflush(f) != 0) return fail_close(f);
+      if (fclose(f) != 0) return 1;
+      f = nullptr;
+    }
+    if (!f) {
+      snprintf(name, sizeof(name), "/%04u-%03u", 1u, ++piece);
+      f = fopen((base + name).c_str(), "wb");
+      if (!f) return 1;
+      inPiece = 0;
+    }
+    Offt &x = index[a];
+    if (x.numOlaps == 0) {
+      x.slice     = 1;
+      x.piece     = (uint16_t)piece;
+      x.offset    = (uint32_t)inPiece;
+      x.overlapID = i;
+    }
+    x.numOlaps++;
+    bgnID = std::min(bgnID, a);
+    endID = std::max(endID, a);
+    if (!write_all(f, r + 1, 5 * sizeof(uint32_t))) return fail_close(f);
+    inPiece++;
+
+    // The record's overlap score (ovOverlap::overlapScore, ovOverlap.H:243-247):
+    // 16384 x identity x (aligned A bases / A length), identity = 1 - evalue / 1e5.
+    const uint64_t d0  = ((uint64_t)r[2] << 32) | r[3];
+    const uint32_t ev  = (uint32_t)((d0 >> 42) & 0xffff);
+    const uint32_t len = readLen[a - 1];
+    const uint32_t al  = len - (uint32_t)(d0 & 0x1fffff) - (uint32_t)((d0 >> 21) & 0x1fffff);
+    scores.push_back((uint16_t)std::floor(16384.0 * (1 - ev / 100000.0) * al / len));
+    if (i + 1 == nRecords || rec[6 * (i + 1)] != a) {
+      prof[a] = score_profile(scores);
+      scores.clear();
+    }
+  }
+  if (f) {
+    if (fflush(f) != 0) return fail_close(f);
+    if (fclose(f) != 0) return 1;
+  }
+
+  if (save_file(base + "/index", index.data(), index.size() * sizeof(Offt))) return 1;
+
+  // statistics (ovStoreHistogram::saveHistogram, ovStoreHistogram.C:135-168): maxID,
+  // first and last ID of the profile array (0 and maxID), the profiles.  No file when
+  // the store holds no overlap.
+  if (nRecords) {
+    std::vector<uint8_t> st(12 + prof.size() * sizeof(ScoreProfile));
+    const uint32_t       hdr[3] = {maxID, 0, maxID};
+    memcpy(st.data(), hdr, 12);
+    memcpy(st.data() + 12, prof.data(), prof.size() * sizeof(ScoreProfile));
+    if (save_file(base + "/statistics", st.data(), st.size())) return 1;
+  }
+
+  // info (ovStoreInfo, ovStore.H:39-137): magic "canu:OVS", version 4, read-length bits,
+  // first and last read ID with overlaps, maxID, records.
+  struct Info {
+    uint64_t magic, version;
+    uint32_t readLenBits, bgnID, endID, maxID;
+    uint64_t numOlaps;
+  };
+  static_assert(sizeof(Info) == 40, "info layout");
+  const Info info = {0x53564f3a756e6163ull, 4, 21, bgnID, endID, maxID, nRecords};
+  return save_file(base + "/info", &info, sizeof(info));
 }
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 // oic_store_build -- the overlap-store build's record pass on the GPU.
 //
-//   oic_store_build -O out -S reads.seqdb [-e maxErate] [--gpu-device d] in1.ovb [in2.ovb ...]
+//   oic_store_build -O out -S reads.seqdb [-e maxErate] [--store dir.ovlStore] [--gpu-device d]
+//                   in1.ovb [in2.ovb ...]
 //
 // canu's ovStoreBuild (src/stores/ovStoreBuild.C) reads the overlapper's .ovb files,
 // filters them (ovStoreFilter), adds every overlap's ID-swapped copy, sorts the kept
@@ -10,11 +11,12 @@
 //   out.ovb    the sorted records, in ovFile's snappy-framed full-record format;
 //   out.index  uint64 per read ID 0..maxID + 1: the index of the read's first record as
 //              the a read (the last entry is the record count), i.e. each read's slice.
+//   --store    also the overlap-store directory canu's own store writer makes from those
+//              records (info, index, data files 0001-NNN, statistics; oic_ovstore_write),
+//              which canu's ovStore reader opens.
 // It prints the filter summary ovStoreBuild prints (ovStoreBuild.C:222-240).
 // Differences: the inputs are listed on the command line (canu passes a store
-// configuration file, -C), and the two files above stand in for canu's store directory,
-// whose layout comes from the absent meryl-utility file routines.  Exit status 0 on
-// success, 1 on any failure.
+// configuration file, -C).  Exit status 0 on success, 1 on any failure.
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
@@ -27,7 +29,7 @@
 #include "oic_seqdb.h"
 
 int main(int argc, char **argv) {
-  const char              *outName = nullptr, *seqName = nullptr;
+  const char              *outName = nullptr, *seqName = nullptr, *storeDir = nullptr;
   double                   maxErate = 1.0;
   int                      device   = 0;
   std::vector<const char *> inputs;
@@ -35,6 +37,7 @@ int main(int argc, char **argv) {
     if (!strcmp(argv[a], "-O") && a + 1 < argc) outName = argv[++a];
     else if (!strcmp(argv[a], "-S") && a + 1 < argc) seqName = argv[++a];
     else if (!strcmp(argv[a], "-e") && a + 1 < argc) maxErate = atof(argv[++a]);
+    else if (!strcmp(argv[a], "--store") && a + 1 < argc) storeDir = argv[++a];
     else if (!strcmp(argv[a], "--gpu-device") && a + 1 < argc) device = atoi(argv[++a]);
     else if (argv[a][0] == '-') {
       fprintf(stderr, "%s: unknown option '%s'.\n", argv[0], argv[a]);
@@ -42,7 +45,9 @@ int main(int argc, char **argv) {
     } else inputs.push_back(argv[a]);
   }
   if (!outName || !seqName || inputs.empty()) {
-    fprintf(stderr, "usage: %s -O out -S reads.seqdb [-e maxErate] [--gpu-device d] in1.ovb [in2.ovb ...]\n",
+    fprintf(stderr,
+            "usage: %s -O out -S reads.seqdb [-e maxErate] [--store dir.ovlStore] [--gpu-device d] in1.ovb "
+            "[in2.ovb ...]\n",
             argv[0]);
     return 1;
   }
@@ -51,7 +56,9 @@ int main(int argc, char **argv) {
     fprintf(stderr, "Failed to load read container '%s'\n", seqName);
     return 1;
   }
-  const uint32_t maxID = db.nReads;
+  const uint32_t        maxID = db.nReads;
+  std::vector<uint32_t> readLen(maxID);
+  for (uint32_t i = 0; i < maxID; i++) readLen[i] = db.index[i].length;
   oic_seqdb_free(&db);
 
   std::vector<uint32_t> words;
@@ -98,6 +105,15 @@ int main(int argc, char **argv) {
   if (!ok) {
     fprintf(stderr, "Failed to write '%s': %s\n", idx.c_str(), strerror(errno));
     return 1;
+  }
+  if (storeDir) {
+    const int wr = oic_ovstore_write(storeDir, out.data(), nOut, readLen.data(), maxID, 0);
+    if (wr) {
+      fprintf(stderr, "Failed to write the overlap store '%s'%s%s\n", storeDir, wr == 1 ? ": " : "",
+              wr == 1 ? strerror(errno) : ": records out of order or outside the reads");
+      return 1;
+    }
+    fprintf(stderr, "Created ovStore '%s' with %llu overlaps.\n", storeDir, (unsigned long long)nOut);
   }
   fprintf(stderr, "%llu overlaps in %s; index %s\nBye.\n", (unsigned long long)nOut, ovb.c_str(), idx.c_str());
   return 0;

@@ -58,6 +58,35 @@ int oic_oc_read(const char *path, uint64_t *nOlaps, uint32_t *opr, uint32_t maxR
  * and their .oc files are summed into outOvb's .oc. */
 int oic_merge_outputs(const char *outOvb, const char *const *inputs, uint32_t n);
 
+/* Records per data file of an overlap store (OVFILE_MAX_OVERLAPS, src/stores/
+ * ovStoreFile.H:27: 1 GiB of 20-byte records). */
+#define OIC_OVSTORE_MAX_PER_FILE 53687091u
+
+/* Write an overlap-store directory as canu's sequential store writer lays it out
+ * (ovStoreWriter, src/stores/ovStoreWriter.C:25-130), the last step of ovStoreBuild
+ * (src/stores/ovStoreBuild.C:255-270), so that canu's ovStore reader
+ * (src/stores/ovStore.C) opens it:
+ *   dir/info        ovStoreInfo (ovStore.H:39-137): uint64 magic "canu:OVS", uint64
+ *                   version 4, uint32 read-length bits (21), uint32 first and last read
+ *                   ID with overlaps, uint32 maxID, uint64 records;
+ *   dir/index       ovStoreOfft (ovStore.H:140-170) per read ID 0..maxID: uint16 slice
+ *                   (1), uint16 data file, uint32 position of the read's first record in
+ *                   that file, uint32 records, 4 zero bytes, uint64 index of the read's
+ *                   first record in the store;
+ *   dir/0001-NNN    the data files: five uint32 words per record (the record without
+ *                   a_iid); a new file starts at a read's first record once the current
+ *                   one holds more than maxPerFile records (0: OIC_OVSTORE_MAX_PER_FILE);
+ *   dir/statistics  (only with records) uint32 maxID, 0, maxID, then per read ID 0..maxID
+ *                   16 uint16 ranks and 16 uint16 scores sampled from its overlaps' scores
+ *                   sorted decreasing (ovStoreHistogram.C:135-259, the overlap score of
+ *                   ovOverlap.H:243-247).
+ * rec: nRecords store records (six words: a_iid, b_iid, dat[0] >> 32, dat[0] & 0xffffffff,
+ * dat[1] >> 32, dat[1] & 0xffffffff) sorted as oic_store_sort returns them; readLen[i]: the
+ * length of read ID i+1, i < maxID.  Returns 2 for records out of order, IDs outside
+ * 1..maxID or A hangs longer than the A read. */
+int oic_ovstore_write(const char *dir, const uint32_t *rec, uint64_t nRecords, const uint32_t *readLen,
+                      uint32_t maxID, uint64_t maxPerFile);
+
 /* Raw snappy block of src[0..n) into dst (capacity at least oic_snappy_max_length(n));
  * *dstLen gets its length.  The block decodes with any snappy decoder. */
 size_t oic_snappy_max_length(size_t n);

@@ -74,3 +74,28 @@ def test_store_build_tool_on_overlapper_output(built, golden_inputs, tmp_path):
     idx = np.fromfile(prefix + ".index", dtype=np.uint64)
     assert (idx == so.per_read_offsets(ref, n)).all()
     assert f"Saved      {rcnt[0]} unitigging overlaps" in r.stderr
+
+
+def test_store_build_tool_writes_the_overlap_store_directory(built, golden_inputs, tmp_path):
+    """oic_store_build --store: the store directory equals the one the library's store
+    writer makes from the oracle's sorted records (tests/test_ovstore.py pins that writer
+    byte for byte to canu's own ovStoreWriter)."""
+    g = golden_inputs["default"]
+    ln = oic.read_seqdb(g["db"])[1]
+    n = len(ln)
+    o = str(tmp_path / "job.ovb")
+    subprocess.run([built["cli"], "-t", "4", "-k", "22", "--hashbits", "16", "--maxerate", "0.06", "--minlength",
+                    "500", "-h", f"1-{n}", "-r", f"1-{n}", "-o", o, g["db"]], check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    store = str(tmp_path / "asm.ovlStore")
+    r = subprocess.run([os.path.join(oic.BUILD, "oic_store_build"), "-O", str(tmp_path / "store"), "-S", g["db"],
+                        "--store", store, o], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ref, _ = so.store_sort(oic.read_ovb(o), n, 1.0)
+    want = str(tmp_path / "want.ovlStore")
+    oic.write_ovstore(want, ref, ln)
+    names = sorted(os.listdir(want))
+    assert len(ref) > 1000 and names == ["0001-001", "index", "info", "statistics"]
+    assert sorted(os.listdir(store)) == names
+    for f in names:
+        assert open(os.path.join(store, f), "rb").read() == open(os.path.join(want, f), "rb").read(), f
