@@ -73,6 +73,25 @@ def workload_text(a):
     return t
 
 
+L2_NOTE = "inputs (2-bit reads, hash table, seed lists) larger than L2"
+
+
+def seqdb_counts(path):
+    """(reads, bases) of an oic_seqdb container, from its header."""
+    import struct
+    with open(path, "rb") as f:
+        head = f.read(24)
+    n, _, nb = struct.unpack("<IIQ", head[8:24])
+    return n, nb
+
+
+def job_config(a, db, ws):
+    """The line's `config`: what the job is, identical in both arms."""
+    n, nb = seqdb_counts(db)
+    return {"workload": workload_text(a), "scale": a.scale, "reads": n, "bases": nb, "parallelism": f"replicas{ws}",
+            "l2": L2_NOTE}
+
+
 # Nominal INT32 lanes per SM (Blackwell: 128 unified FP32/INT32 lanes).
 INT_LANES_PER_SM = 128
 
@@ -371,8 +390,7 @@ def main():
         line = {"impl": "reference", "metric": "overlaps_per_sec", "value": v, "unit": "overlaps/s", "n_gpus": 0,
                 "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * statistics.mean(s[0] for s in samples),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-                "data": "synthetic", "config": {"workload": workload_text(a),
-                                                "scale": a.scale, "reads": cpu.nReads},
+                "data": "synthetic", "config": job_config(a, db, ws),
                 "cpu_baseline": {"value": v, "unit": "overlaps/s", "cores": cores, "kind": "port",
                                  "sample": f"{nrefs} ref reads (both strands) in chunks of 16 spread over the ID "
                                            f"range, against the first hash block; block build {cpu.build_s:.1f} s "
@@ -524,9 +542,8 @@ def main():
         "metric": "overlaps_per_sec", "value": value, "unit": "overlaps/s", "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_dev_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": workload_text(a), "scale": a.scale, "reads": nReads,
-                   "bases": int(bases.size), "overlaps_per_step": n_ov, "parallelism": f"replicas{ws}",
-                   "l2": "inputs (2-bit reads, hash table, seed lists) larger than L2"},
+        "config": job_config(a, db, ws),
+        "overlaps_per_step": n_ov,
         "dp_cells_per_sec": ws * cells / (ms_dev_max / 1000.0),
         "work": {"seeds": st0["seeds"], "candidate_pairs": pairs, "match_nodes": nodes, "extensions": st0["extensions"],
                  "dp_cells": cells, "dp_rows": st0.get("dpRows"), "slide_bases": slides,

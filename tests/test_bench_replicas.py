@@ -67,3 +67,18 @@ def test_workload_text_says_when_the_skip_list_is_left_out():
         assert without.startswith(wl + ":")
     c1 = bench.workload_text(argparse.Namespace(workload="c1", no_skip_list=False))
     assert c1 == bench.WORKLOAD_TEXT["c1"]
+
+
+def test_both_arms_describe_the_job_with_the_same_config(tmp_path):
+    """The reference arm and the GPU arm build `config` with the same function, from the
+    read container's header and the arguments: same keys, same values."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    import canu_gb300 as oic
+    db = str(tmp_path / "r.seqdb")
+    oic.write_seqdb(db, ["ACGT" * 50, "GATTACA" * 30, "T" * 7])
+    a = argparse.Namespace(workload="c2", no_skip_list=False, scale=0.5)
+    c = bench.job_config(a, db, 2)
+    assert c == {"workload": bench.WORKLOAD_TEXT["c2"], "scale": 0.5, "reads": 3, "bases": 200 + 210 + 7,
+                 "parallelism": "replicas2", "l2": bench.L2_NOTE}
