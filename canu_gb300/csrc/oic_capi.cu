@@ -54,7 +54,10 @@ int binomial_bound(int e, double p, int start) {
       int    coeff = 1, ct = 0;
       for (int k = 0; k < e && 1.0 - sum > 1e-4; k++) {
         sum += coeff * pPow * qPow;
-        coeff *= n - ct;
+        // The reference's int product overflows (C(n, k) * (n - k) past 2^31 for n near
+        // 35 at high error counts) and the table depends on the 32-bit wraparound it
+        // gets; the same wraparound, as a defined unsigned product.
+        coeff = (int)((uint32_t)coeff * (uint32_t)(n - ct));
         coeff /= ++ct;
         pPow *= p;
         qPow /= q;

@@ -179,7 +179,10 @@ static int binomial_bound(int e, double p, int start) {
       for (k = 0; k < e && 1.0 - sum > 1e-4; k++) {
         double x = coeff * pp * qp;
         sum += x;
-        coeff *= n - ct;
+        /* Binomial_Bound.C:63's int product overflows for n near 35 at high error
+           counts and the reference's table depends on the 32-bit wraparound; the same
+           wraparound as a defined unsigned product. */
+        coeff = (int)((uint32_t)coeff * (uint32_t)(n - ct));
         coeff /= ++ct;
         pp *= p;
         qp /= q;
