@@ -205,6 +205,11 @@ int main(int argc, char **argv) {
   }
   if (!canWrite(outName) || !canWrite(ocName) || (statName && !canWrite(statName))) return 1;
 
+  // The skip list is checked before any device work too: a malformed file ends the run
+  // as the reference's Mark_Skip_Kmers does.
+  std::string skipKmers;
+  if (skipFile && readSkipFile(skipFile, P.kmerLen, skipKmers)) return 1;
+
   oic_seqdb db;
   if (oic_seqdb_load(store, &db)) {
     fprintf(stderr, "Failed to load read container '%s'\n", store);
@@ -225,10 +230,8 @@ int main(int argc, char **argv) {
   }
   rc = oic_set_reads(ctx, db.nReads, lib.data(), len.data(), off.data(), db.bases, db.nBases);
   if (!rc && skipFile) {
-    std::string kmers;
-    if (readSkipFile(skipFile, P.kmerLen, kmers)) return 1;
-    rc = oic_set_skip_kmers(ctx, kmers.data(), kmers.size() / P.kmerLen);
-    fprintf(stderr, "\nRead %zu kmers to mark to skip\n\n", kmers.size() / P.kmerLen);
+    rc = oic_set_skip_kmers(ctx, skipKmers.data(), skipKmers.size() / P.kmerLen);
+    fprintf(stderr, "\nRead %zu kmers to mark to skip\n\n", skipKmers.size() / P.kmerLen);
   }
   if (!rc && haveTune) rc = oic_set_tuning(ctx, &tune);
   if (!rc && autotuneRefs) {

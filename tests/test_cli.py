@@ -59,3 +59,17 @@ def test_malformed_read_container_is_rejected(built, tmp_path, damage):
     open(db, "wb").write(bytes(raw))
     r = run(built, "-k", "22", "-o", str(tmp_path / "o.ovb"), db)
     assert r.returncode == 1 and "Failed to load read container" in r.stderr
+
+
+def test_malformed_skip_list_is_rejected_before_device_work(built, tmp_path):
+    """A -k k-mer file whose entries are not k bases long ends the run with the
+    reference's message (Build_Hash_Index.C:222-226), before any device work."""
+    import canu_gb300 as oic
+    db = str(tmp_path / "in.seqdb")
+    oic.write_seqdb(db, ["ACGT" * 300, "TTGCA" * 200])
+    skip = tmp_path / "bad.skip"
+    skip.write_text(">1\n" + "A" * 22 + "\t7\n>2\n" + "ACGT" * 5 + "\t3\n")
+    r = run(built, "-k", "22", "-k", str(skip), "-o", str(tmp_path / "o.ovb"), db)
+    assert r.returncode == 1
+    assert "Short kmer skip kmer '" + "ACGT" * 5 + "' at line 4, expecting length 22 got length 20." in r.stderr
+    assert "oic_create" not in r.stderr
