@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "oic_gpu.h"
 #include "oic_kernels.cuh"
 #include "oic_prims.cuh"
@@ -480,8 +482,18 @@ void launch_cta_bin(oic_ctx *ctx, const oic_tuning &t, const CtaBin &b, uint32_t
 // Seed stage of a batch: the ref reads' seeds replayed into candidate pairs and match
 // runs (dPairs, dNodes), then their filter scores when a filter is set or pairs are
 // collected.  Returns OIC_OK, kRetrySmaller when the batch's output did not fit.
+// A named range on the NVTX timeline for the life of the object: the library's stages
+// by name in Nsight Systems / Nsight Compute; nothing is recorded without such a tool.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &)            = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 int seed_stage(oic_ctx *ctx, const uint32_t *refs, uint32_t nRefs, cudaEvent_t evSeed0, cudaEvent_t evSeed1,
                uint32_t &nPairs, uint32_t &nNodes) {
+  NvtxRange range("oic seed stage");
   const uint32_t nSeg = nRefs * 2;
   CK(ctx->dSegReads.ensure((size_t)nRefs * sizeof(uint32_t)));
   CK(cudaMemcpyAsync(ctx->dSegReads.p, refs, (size_t)nRefs * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
@@ -573,6 +585,7 @@ struct AlignTimes {
 // into `recOut` (appended) and the counters into ctx->stats.
 int align_stage(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning &tn, cudaEvent_t evAln0,
                 cudaEvent_t evAln1, std::vector<uint32_t> &recOut, AlignTimes &at) {
+  NvtxRange range("oic DP stage");
   int rc = OIC_OK;
   const bool useFilter = ctx->filterOn && nPairs > 0;
   CK(cudaMemsetAsync(ctr32(ctx) + cWorkCounter, 0, 4 * sizeof(uint32_t), ctx->st));   // work, aln ovf, err, rec total
@@ -773,6 +786,7 @@ template <typename T> void key_add(std::vector<uint8_t> &k, const T &v) {
 // after the launch; the rare large-arena rerun runs outside the graph.
 int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_tuning &tn, cudaEvent_t evAln0,
                       cudaEvent_t evAln1, std::vector<uint32_t> &recOut, AlignTimes &at) {
+  NvtxRange range("oic DP stage (graph)");
   int rc = OIC_OK;
   const bool     useFilter = ctx->filterOn && nPairs > 0;
   const bool     coll      = ctx->collect != 0;
@@ -1319,6 +1333,7 @@ int oic_set_skip_kmers(oic_ctx *ctx, const char *kmers, uint64_t nKmers) {
 }
 
 int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *lastLoaded) {
+  NvtxRange range("oic hash block");
   if (!ctx) return OIC_ERR_ARG;
   if (ctx->nReads == 0) return fail(ctx, OIC_ERR_STATE, "no reads loaded");
   cudaSetDevice(ctx->device);
@@ -1482,6 +1497,7 @@ int oic_load_hash_block(oic_ctx *ctx, uint32_t bgnID, uint32_t endID, uint32_t *
 }
 
 int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
+  NvtxRange range("oic ref reads");
   if (!ctx) return OIC_ERR_ARG;
   if (!ctx->haveBlock) return fail(ctx, OIC_ERR_STATE, "no hash block loaded");
   cudaSetDevice(ctx->device);
@@ -1541,6 +1557,7 @@ int oic_run_refs(oic_ctx *ctx, uint32_t bgnRefID, uint32_t endRefID) {
 }
 
 int oic_run(oic_ctx *ctx) {
+  NvtxRange range("oic run");
   if (!ctx) return OIC_ERR_ARG;
   if (ctx->nReads == 0) return fail(ctx, OIC_ERR_STATE, "no reads loaded");
   oic_params G = ctx->P;
