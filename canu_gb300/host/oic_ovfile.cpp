@@ -396,6 +396,7 @@ int oic_ovstore_write(const char *dir, const uint32_t *rec, uint64_t nRecords, c
                       uint32_t maxID, uint64_t maxPerFile) {
   if (!dir || (!rec && nRecords) || (!readLen && maxID)) return 2;
   if (maxPerFile == 0) maxPerFile = OIC_OVSTORE_MAX_PER_FILE;
+  if (maxPerFile > 0x7fffffffull) return 2;   // offsets in a data file are 32-bit in the index
 
   // The records must be a store's: IDs within 1..maxID, in (a_iid, b_iid, data) order,
   // with A hangs inside the A read (the score divides by the read's length).
@@ -447,6 +448,10 @@ int oic_ovstore_write(const char *dir, const uint32_t *rec, uint64_t nRecords, c
       inPiece = 0;
     }
     Offt &x = index[a];
+    if (inPiece > 0xffffffffull || x.numOlaps == 0xffffffffu) {   // past the index's 32-bit fields
+      fclose(f);
+      return 2;
+    }
     if (x.numOlaps == 0) {
       x.slice     = 1;
       x.piece     = (uint16_t)piece;

@@ -83,7 +83,8 @@ int oic_merge_outputs(const char *outOvb, const char *const *inputs, uint32_t n)
  * rec: nRecords store records (six words: a_iid, b_iid, dat[0] >> 32, dat[0] & 0xffffffff,
  * dat[1] >> 32, dat[1] & 0xffffffff) sorted as oic_store_sort returns them; readLen[i]: the
  * length of read ID i+1, i < maxID.  Returns 2 for records out of order, IDs outside
- * 1..maxID or A hangs longer than the A read. */
+ * 1..maxID, A hangs longer than the A read or maxPerFile above 2^31 - 1 (the index holds
+ * 32-bit offsets); 1 when a file cannot be written (files already written stay). */
 int oic_ovstore_write(const char *dir, const uint32_t *rec, uint64_t nRecords, const uint32_t *readLen,
                       uint32_t maxID, uint64_t maxPerFile);
 
