@@ -482,6 +482,23 @@ void launch_cta_bin(oic_ctx *ctx, const oic_tuning &t, const CtaBin &b, uint32_t
 // Seed stage of a batch: the ref reads' seeds replayed into candidate pairs and match
 // runs (dPairs, dNodes), then their filter scores when a filter is set or pairs are
 // collected.  Returns OIC_OK, kRetrySmaller when the batch's output did not fit.
+// Two CUDA events destroyed with the object, so that every return (the error returns
+// included) releases them.  ok() is false when either could not be created.
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    if (cudaEventCreate(&a) != cudaSuccess) a = nullptr;
+    if (cudaEventCreate(&b) != cudaSuccess) b = nullptr;
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  bool ok() const { return a && b; }
+  EventPair(const EventPair &)            = delete;
+  EventPair &operator=(const EventPair &) = delete;
+};
+
 // A named range on the NVTX timeline for the life of the object: the library's stages
 // by name in Nsight Systems / Nsight Compute; nothing is recorded without such a tool.
 struct NvtxRange {
@@ -950,9 +967,9 @@ int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_
     AlignCaps   capsH;
     WarpScratch wsH;
     if ((rc = ensure_group_scratch(ctx, tn, true, ctasH, capsH, wsH))) return rc;
-    cudaEvent_t h0, h1;
-    cudaEventCreate(&h0);
-    cudaEventCreate(&h1);
+    EventPair hev;
+    if (!hev.ok()) return fail(ctx, OIC_ERR_CUDA, "cudaEventCreate failed");
+    const cudaEvent_t h0 = hev.a, h1 = hev.b;
     cudaEventRecord(h0, ctx->st);
     launch_align_group((int)std::max<uint32_t>(tn.wideThreads, 512), (int)tn.wideTile, capsH.bandW,
                        (int)std::min<uint32_t>(ctasH, o), ctx->R, ctx->T, ctx->dp, ctx->dEml.as<int>(),
@@ -967,8 +984,6 @@ int align_stage_graph(oic_ctx *ctx, uint32_t nPairs, uint32_t nNodes, const oic_
     rc = sync_check(ctx, "align kernel (large arena)");
     float hm = 0;
     cudaEventElapsedTime(&hm, h0, h1);
-    cudaEventDestroy(h0);
-    cudaEventDestroy(h1);
     if (rc) return rc;
     at.msWide += hm;
     at.pairsWide += o;
@@ -1256,9 +1271,9 @@ int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const ui
   ctx->wordOff[nReads] = w;
   const uint64_t nWords = w + 4;   // spare words: 32-base windows and staged tiles past the last read
 
-  cudaEvent_t r0, r1;
-  cudaEventCreate(&r0);
-  cudaEventCreate(&r1);
+  EventPair rev;
+  if (!rev.ok()) return fail(ctx, OIC_ERR_CUDA, "cudaEventCreate failed");
+  const cudaEvent_t r0 = rev.a, r1 = rev.b;
   cudaEventRecord(r0, ctx->st);
   CK(ctx->dFwd.ensure(nWords * 8));
   CK(ctx->dRc.ensure(nWords * 8));
@@ -1296,8 +1311,6 @@ int oic_set_reads(oic_ctx *ctx, uint32_t nReads, const uint32_t *libID, const ui
   cudaEventSynchronize(r1);
   float msR = 0;
   cudaEventElapsedTime(&msR, r0, r1);
-  cudaEventDestroy(r0);
-  cudaEventDestroy(r1);
   ctx->stats.msReads = msR;
   ReadsDev &R = ctx->R;
   R.fwd     = ctx->dFwd.as<u64>();
