@@ -9,7 +9,7 @@
 
 namespace oic {
 
-unsigned long long g_launches = 0;
+thread_local unsigned long long g_launches = 0;
 
 namespace {
 

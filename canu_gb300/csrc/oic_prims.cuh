@@ -8,8 +8,10 @@
 
 namespace oic {
 
-// Kernels launched by this library since load (for launch accounting).
-extern unsigned long long g_launches;
+// Kernels this host thread has launched through the library (for launch accounting).
+// Per thread: a context is driven by one thread at a time, so the difference across a
+// call counts that call's launches even while other threads drive other contexts.
+extern thread_local unsigned long long g_launches;
 
 // Scratch bytes oic_scan_u32 needs for n elements.
 size_t scan_u32_scratch(uint64_t n);
