@@ -520,6 +520,11 @@ def main():
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     int_peak = 152 * INT_LANES_PER_SM * sm_mhz * 1e6 / 1e12
     int_ops = 6 * cells + slides / 16.0
+    # Instruction issue, the one-warp DP's binding resource: 15.85 warp instructions per
+    # DP cell (ncu smsp__inst_executed.sum of the same 1/50-scale c2 launch) against 152
+    # SMs x 4 schedulers x one warp instruction per cycle.
+    issue_peak = 152 * 4 * sm_mhz * 1e6 / 1e9
+    issue_ach = 15.85 * cells / (ms_align / 1000.0) / 1e9
     # The memory stages by the byte model of the hash build and probe: build 0.25 B per
     # base read + 12 B per k-mer written (8 B key, 4 B position), and separately the sort
     # passes (6 passes x 24 B per k-mer); probe 2 strands x (0.25 B per base + one 32 B
@@ -561,6 +566,11 @@ def main():
                                  "frac": int_ops / (ms_align / 1000.0) / 1e12 / int_peak,
                                  "basis": "6 INT ops per DP cell + 1/16 per slide base; peak = 152 SMs x 128 "
                                           "INT32 lanes x median SM clock"},
+                     "issue": {"achieved_g_warp_inst_per_s": issue_ach, "peak_g_warp_inst_per_s": issue_peak,
+                               "frac": issue_ach / issue_peak,
+                               "basis": "15.85 warp instructions per DP cell (ncu, one-warp DP kernel, 1/50-scale "
+                                        "c2 launch: profiles/align_kernel_c2_scale0.02_ncu.md) x this job's DP "
+                                        "cells / DP stage time; peak = 152 SMs x 4 schedulers x median SM clock"},
                      "hash": stage_roof(hash_bytes, ms_hash, "0.25 B/base + 12 B/k-mer (sort passes excluded)"),
                      "hash_with_sort": stage_roof(hash_bytes + sort_passes * 24 * n_kmers, ms_hash,
                                                   f"as hash + {sort_passes} radix passes x 24 B/k-mer",
