@@ -30,7 +30,7 @@ EXPORTS = (
     "oic_clear_overlaps", "oic_get_stats", "oic_extend_batch", "oic_get_match_limit", "oic_last_error",
     "oic_extend_batch_noalloc", "oic_set_filter", "oic_collect_pairs", "oic_num_pairs", "oic_get_pairs",
     "oic_clear_pairs", "oic_mlp_forward", "oic_mlp_backward", "oic_mlp_adam", "oic_set_tuning", "oic_get_tuning",
-    "oic_autotune", "oic_count_kmers", "oic_store_sort",
+    "oic_autotune", "oic_count_kmers", "oic_store_sort", "oic_stats_json",
 )
 # Output files (include/oic_ovfile.h): host code of the same library, no GPU needed.
 OVFILE_EXPORTS = (
@@ -89,6 +89,16 @@ class OicStats(ctypes.Structure):
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
+    def to_json(self):
+        """oic_stats_json: the counters, device times and rates as JSON text."""
+        lib, n = library(), ctypes.c_size_t()
+        lib.oic_stats_json(ctypes.byref(self), None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        rc = lib.oic_stats_json(ctypes.byref(self), buf, n.value + 1, ctypes.byref(n))
+        if rc:
+            raise OicError(rc, "oic_stats_json")
+        return buf.value.decode()
+
 
 class FilterDomain(ctypes.Structure):
     """oic_filter_domain: the parameters a filter network was trained under."""
@@ -137,6 +147,7 @@ def library():
         lib.oic_fetch_overlaps.argtypes = [vp, vp, U64, P(U64)]
         lib.oic_clear_overlaps.argtypes = [vp]
         lib.oic_get_stats.argtypes = [vp, P(OicStats)]
+        lib.oic_stats_json.argtypes = [P(OicStats), ctypes.c_char_p, ctypes.c_size_t, P(ctypes.c_size_t)]
         lib.oic_extend_batch.argtypes = [vp, U32] + [vp] * 9
         lib.oic_get_match_limit.argtypes = [vp, vp, U32, P(U32)]
         lib.oic_extend_batch_noalloc.argtypes = [vp, U32, vp, vp, vp, vp, vp]

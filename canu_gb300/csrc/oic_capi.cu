@@ -1648,6 +1648,37 @@ int oic_get_stats(oic_ctx *ctx, oic_stats *st) {
   return OIC_OK;
 }
 
+int oic_stats_json(const oic_stats *s, char *buf, size_t cap, size_t *len) {
+  if (!s || !len || (!buf && cap)) return OIC_ERR_ARG;
+  const double ovps = s->msTotal > 0 ? (double)s->totalOverlaps / (s->msTotal / 1000.0) : 0.0;
+  const double dpps = s->msAlign > 0 ? (double)s->dpCells / (s->msAlign / 1000.0) : 0.0;
+  const int n = snprintf(
+      buf, cap,
+      "{\"kmerHitsWithoutOlap\": %llu, \"kmerHitsWithOlap\": %llu, \"kmerHitsSkipped\": %llu, "
+      "\"multiOverlap\": %llu, \"totalOverlaps\": %llu, \"containedOverlaps\": %llu, "
+      "\"dovetailOverlaps\": %llu, \"badShortWindow\": %llu, \"badLongWindow\": %llu, \"dpCells\": %llu, "
+      "\"slideBases\": %llu, \"extensions\": %llu, \"seeds\": %llu, \"candidatePairs\": %llu, \"nodes\": %llu, "
+      "\"dpRows\": %llu, \"nHashBlocks\": %u, \"msHash\": %.6f, \"msSeed\": %.6f, \"msAlign\": %.6f, "
+      "\"msTotal\": %.6f, \"msReads\": %.6f, \"kernelLaunches\": %llu, \"dpCellsNoOverlap\": %llu, "
+      "\"filteredPairs\": %llu, \"msFilter\": %.6f, \"msNarrow\": %.6f, \"msWide\": %.6f, "
+      "\"pairsNarrow\": %llu, \"pairsWide\": %llu, \"cellsWide\": %llu, \"graphLaunches\": %llu, "
+      "\"overlapsPerSec\": %.3f, \"dpCellsPerSec\": %.3f}",
+      (unsigned long long)s->kmerHitsWithoutOlap, (unsigned long long)s->kmerHitsWithOlap,
+      (unsigned long long)s->kmerHitsSkipped, (unsigned long long)s->multiOverlap,
+      (unsigned long long)s->totalOverlaps, (unsigned long long)s->containedOverlaps,
+      (unsigned long long)s->dovetailOverlaps, (unsigned long long)s->badShortWindow,
+      (unsigned long long)s->badLongWindow, (unsigned long long)s->dpCells, (unsigned long long)s->slideBases,
+      (unsigned long long)s->extensions, (unsigned long long)s->seeds, (unsigned long long)s->candidatePairs,
+      (unsigned long long)s->nodes, (unsigned long long)s->dpRows, s->nHashBlocks, s->msHash, s->msSeed,
+      s->msAlign, s->msTotal, s->msReads, (unsigned long long)s->kernelLaunches,
+      (unsigned long long)s->dpCellsNoOverlap, (unsigned long long)s->filteredPairs, s->msFilter, s->msNarrow,
+      s->msWide, (unsigned long long)s->pairsNarrow, (unsigned long long)s->pairsWide,
+      (unsigned long long)s->cellsWide, (unsigned long long)s->graphLaunches, ovps, dpps);
+  if (n < 0) return OIC_ERR_ARG;
+  *len = (size_t)n;
+  return (size_t)n < cap ? OIC_OK : OIC_ERR_ARG;
+}
+
 int oic_set_filter(oic_ctx *ctx, const uint16_t *params, float threshold, float fullThreshold, uint32_t extBudget,
                    const oic_filter_domain *trainedOn) {
   if (!ctx) return OIC_ERR_ARG;

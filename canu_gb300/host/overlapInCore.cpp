@@ -19,7 +19,9 @@
 //     (narrowArena, wideMinLen, wideThreads, wideTile, wideBandW, wideCtas, wideArena,
 //     forceWide, noGraph, wideMode), and --gpu-autotune <n> times the DP grid on the first n ref reads
 //     against the first hash block and keeps the fastest configuration (oic_autotune).
-//     Neither changes the records.
+//     Neither changes the records;
+//   * --gpu-metrics <file> writes the run's counters, device times and rates as JSON
+//     (oic_stats_json), a sidecar the reference does not have.
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -53,6 +55,7 @@ void usage(const char *prog) {
   fprintf(stderr, "  -partial -h a-b -H a-b -r a-b -R a-b -k <int|file> -m -u -z -t <n>\n");
   fprintf(stderr, "  --hashbits n --hashdatalen n --hashload f --maxerate f --alignnoise f\n");
   fprintf(stderr, "  --minlength n --minkmers -o out.ovb -s out.stats [--gpu-device d] [--ovb-raw]\n");
+  fprintf(stderr, "  [--gpu-metrics metrics.json]\n");
   fprintf(stderr, "  [--gpu-tune key=value,...] [--gpu-autotune nRefs]\n");
 }
 
@@ -136,7 +139,7 @@ int main(int argc, char **argv) {
   oic_params P;
   oic_default_params(&P);
   P.numThreads = 1;
-  const char *store = nullptr, *outName = nullptr, *statName = nullptr, *skipFile = nullptr;
+  const char *store = nullptr, *outName = nullptr, *statName = nullptr, *skipFile = nullptr, *metricsName = nullptr;
   int         device = 0, err = 0;
   bool        snappy = true, haveTune = false;
   oic_tuning  tune{};
@@ -179,6 +182,7 @@ int main(int argc, char **argv) {
     else if (!strcmp(o, "--alignnoise")) P.alignNoise = strtof(nxt(), nullptr);
     else if (!strcmp(o, "-z")) P.useHopelessCheck = 0;
     else if (!strcmp(o, "--gpu-device")) device = atoi(nxt());
+    else if (!strcmp(o, "--gpu-metrics")) metricsName = nxt();
     else if (!strcmp(o, "--ovb-snappy")) snappy = true;
     else if (!strcmp(o, "--ovb-raw")) snappy = false;
     else if (!strcmp(o, "--gpu-tune")) {
@@ -203,7 +207,9 @@ int main(int argc, char **argv) {
     fprintf(stderr, "Output name '%s' is too long\n", outName);
     return 1;
   }
-  if (!canWrite(outName) || !canWrite(ocName) || (statName && !canWrite(statName))) return 1;
+  if (!canWrite(outName) || !canWrite(ocName) || (statName && !canWrite(statName)) ||
+      (metricsName && !canWrite(metricsName)))
+    return 1;
 
   // The skip list is checked before any device work too: a malformed file ends the run
   // as the reference's Mark_Skip_Kmers does.
@@ -289,6 +295,20 @@ int main(int argc, char **argv) {
   if (w) {
     fprintf(stderr, "Failed to write the stats to '%s': %s\n", statName ? statName : "stderr", strerror(errno));
     return 1;
+  }
+
+  if (metricsName) {   // the JSON sidecar: counters, device times, rates
+    size_t len = 0;
+    oic_stats_json(&st, nullptr, 0, &len);
+    std::string js(len + 1, '\0');
+    FILE *M  = fopen(metricsName, "w");
+    bool  ok = M && oic_stats_json(&st, &js[0], js.size(), &len) == OIC_OK && fwrite(js.data(), 1, len, M) == len &&
+              fputc('\n', M) != EOF;
+    ok = (M && fclose(M) == 0) && ok;
+    if (!ok) {
+      fprintf(stderr, "Failed to write the metrics to '%s': %s\n", metricsName, strerror(errno));
+      return 1;
+    }
   }
 
   fprintf(stderr, "GPU: %lu overlaps; %lu seeds, %lu pairs, %lu extensions, %lu DP cells (%lu in pairs without "

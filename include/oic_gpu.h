@@ -123,6 +123,15 @@ int oic_clear_overlaps(oic_ctx *ctx);
 
 int oic_get_stats(oic_ctx *ctx, oic_stats *st);
 
+/* No counterpart in the reference (its only report is the -s stats text,
+ * overlapInCore.C:550-558).  The counters and device times of *st as one JSON object
+ * (keys as the oic_stats field names) plus the derived rates overlapsPerSec
+ * (totalOverlaps over msTotal) and dpCellsPerSec (dpCells over msAlign; 0 when a time
+ * is 0): the metrics sidecar of a run.  Host code only.  Writes at most cap bytes
+ * (NUL included) to buf and sets *len to the text's length without the NUL; returns
+ * OIC_ERR_ARG when cap is too small (*len still says how much is needed). */
+int oic_stats_json(const oic_stats *st, char *buf, size_t cap, size_t *len);
+
 /* Batched Extend_Alignment (prefixEditDistance-extend.C:36-183) over nAlign
  * independent problems, for direct testing of the DP kernel.  Problem i aligns the
  * exact match (mStart[i] in S, mOffset[i] in T, mLen[i]) of S = read sRead[i] on

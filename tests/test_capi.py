@@ -65,3 +65,27 @@ def test_bad_parameters_rejected(built):
     assert lib.oic_create(ctypes.byref(p), 0, ctypes.byref(ctx)) == oic.OIC_ERR_ARG
     p = oic.default_params(kmerLen=40)
     assert lib.oic_create(ctypes.byref(p), 0, ctypes.byref(ctx)) == oic.OIC_ERR_ARG
+
+
+def test_stats_json_carries_every_counter_and_the_rates(built):
+    """oic_stats_json (host code): every oic_stats field by name, and overlaps/s and DP
+    cells/s from the device times; a buffer one byte short is refused with the size."""
+    import ctypes
+    import json
+    s = oic.OicStats()
+    for i, (name, typ) in enumerate(s._fields_):
+        setattr(s, name, (1.5 * (i + 1)) if typ is ctypes.c_double else (i + 1) * 1000003)
+    s.totalOverlaps, s.msTotal, s.dpCells, s.msAlign = 12345, 250.0, 9 * 10**11, 4500.0
+    d = json.loads(s.to_json())
+    for name, typ in s._fields_:
+        if name != "reserved":
+            assert d[name] == getattr(s, name), name
+    assert d["overlapsPerSec"] == pytest.approx(12345 / 0.25)
+    assert d["dpCellsPerSec"] == pytest.approx(9e11 / 4.5)
+    lib, n = oic.library(), ctypes.c_size_t()
+    assert lib.oic_stats_json(ctypes.byref(s), None, 0, ctypes.byref(n)) == oic.OIC_ERR_ARG and n.value > 0
+    buf = ctypes.create_string_buffer(n.value)
+    assert lib.oic_stats_json(ctypes.byref(s), buf, n.value, ctypes.byref(n)) == oic.OIC_ERR_ARG
+    s.msTotal = s.msAlign = 0.0
+    d = json.loads(s.to_json())
+    assert d["overlapsPerSec"] == 0 and d["dpCellsPerSec"] == 0

@@ -73,3 +73,13 @@ def test_malformed_skip_list_is_rejected_before_device_work(built, tmp_path):
     assert r.returncode == 1
     assert "Short kmer skip kmer '" + "ACGT" * 5 + "' at line 4, expecting length 22 got length 20." in r.stderr
     assert "oic_create" not in r.stderr
+
+
+def test_unwritable_metrics_file_fails_before_device_work(built, tmp_path):
+    import canu_gb300 as oic
+    db = str(tmp_path / "in.seqdb")
+    oic.write_seqdb(db, ["ACGT" * 300, "TTGCA" * 200])
+    r = run(built, "-k", "22", "--gpu-metrics", str(tmp_path / "no_such_dir" / "m.json"), "-o",
+            str(tmp_path / "o.ovb"), db)
+    assert r.returncode == 1 and "Failed to open" in r.stderr and "m.json" in r.stderr
+    assert "oic_create" not in r.stderr
