@@ -99,9 +99,21 @@ def build_synth():
     return syn
 
 
+def build_importer():
+    """The FASTA / FASTQ importer into the read container (host only; no CUDA)."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "host", "oic_seqdb_import.cpp")
+    exe = os.path.join(OUT, "oic_seqdb_import")
+    if _stale(exe, [src, os.path.join(INC, "oic_seqdb.h")]):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INC, "-o", exe, src])
+    return exe
+
+
 def build_tools():
     """The command-line tools, linked against liboic_gpu.so: overlapInCore (the drop-in),
-    oic_kmers (frequent k-mers) and oic_merge (merges independent jobs' outputs)."""
+    oic_kmers (frequent k-mers), oic_merge (merges independent jobs' outputs) and
+    oic_store_build (the overlap store); and, host only, the read generator and the
+    FASTA / FASTQ importer (oic_seqdb_import)."""
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
     cuda_home = os.path.dirname(os.path.dirname(os.path.realpath(nv)))
@@ -118,6 +130,7 @@ def build_tools():
     with ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
         list(ex.map(_run, jobs))
     syn = build_synth()
+    build_importer()
     return os.path.join(OUT, "overlapInCore"), syn
 
 

@@ -87,3 +87,22 @@ def test_read_generator_under_sanitizers(san_dir, tmp_path):
         assert sha256(db) == c["seqdb_sha256"]
         if c["skip_sha256"]:
             assert sha256(skip) == c["skip_sha256"]
+
+
+def test_read_importer_under_sanitizers(san_dir, tmp_path):
+    """oic_seqdb_import on well-formed, wrapped, mixed-case and malformed FASTA / FASTQ."""
+    exe = build(["g++", "-std=c++17", "-I" + os.path.join(ROOT, "include")] + SAN +
+                [os.path.join(ROOT, "canu_gb300", "host", "oic_seqdb_import.cpp")], os.path.join(san_dir, "imp"))
+    good = tmp_path / "g.fa"
+    good.write_bytes(b">a x\r\nacgtRYKM\r\n\r\n>b\n" + b"ACGT" * 5000 + b"\n>c\n\n")
+    fq = tmp_path / "g.fq"
+    fq.write_text("@q1\nACGT\nAC\n+\n@@@@\nII\n@q2\nNNNN\n+\n####\n")
+    r = subprocess.run([exe, "-o", str(tmp_path / "o.seqdb"), str(good), str(fq)], stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, env=ENV)
+    assert r.returncode == 0 and clean(r.stderr), r.stderr[-3000:]
+    for content in ("@q\nACGT\n+\nII\n", "@q\nAC", ">", "xyz\n", ""):
+        bad = tmp_path / "bad.fq"
+        bad.write_text(content)
+        r = subprocess.run([exe, "-o", str(tmp_path / "b.seqdb"), str(bad)], stdout=subprocess.PIPE,
+                           stderr=subprocess.PIPE, text=True, env=ENV)
+        assert r.returncode in (0, 1) and clean(r.stderr), (content, r.stderr[-3000:])
