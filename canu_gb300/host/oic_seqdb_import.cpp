@@ -16,8 +16,10 @@
 //     the sqStore's readNames.txt maps IDs to names.
 // FASTA records may wrap over several lines; FASTQ records may wrap their sequence and
 // quality (the quality must be as long as the sequence).  Blank lines and Windows line
-// ends are accepted.  Exit status 0 on success, 1 on an unreadable, malformed or
-// unwritable file (nothing is written then).
+// ends are accepted.  A read longer than 2^21 - 1 bases (what a read store holds) is an
+// error.  Exit status 0 on success, 1 on an unreadable, malformed or unwritable file
+// (nothing is written then).
+#include <algorithm>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
@@ -35,15 +37,20 @@ struct Reads {
   std::string              bases;
 };
 
-// One line without its end of line ('\n', '\r\n'); false at end of file.
+// One line without its end of line ('\n', '\r\n'); false at end of file.  Reads in
+// 64 KiB pieces (fgets), so long sequence lines cost one call per piece.
 bool get_line(FILE *f, std::string &line) {
   line.clear();
-  int c;
+  char buf[1 << 16];
   bool any = false;
-  while ((c = fgetc(f)) != EOF) {
-    any = true;
-    if (c == '\n') break;
-    line.push_back((char)c);
+  while (fgets(buf, sizeof(buf), f)) {
+    any            = true;
+    const size_t n = strlen(buf);
+    if (n > 0 && buf[n - 1] == '\n') {
+      line.append(buf, n - 1);
+      break;
+    }
+    line.append(buf, n);
   }
   if (!line.empty() && line.back() == '\r') line.pop_back();
   return any;
@@ -71,10 +78,13 @@ std::string first_word(const std::string &header) {
   return header.substr(b, e - b);
 }
 
+// The longest read a store holds (AS_MAX_READLEN, 21-bit read positions).
+constexpr size_t kMaxReadLen = (1u << 21) - 1;
+
 void keep(Reads &r, uint32_t lib, const std::string &name, const std::string &seq, uint32_t minLen) {
   if (seq.size() < minLen) return;
   r.lib.push_back(lib);
-  r.len.push_back((uint32_t)seq.size());
+  r.len.push_back((uint32_t)std::min<size_t>(seq.size(), 0xffffffffu));
   r.names.push_back(name);
   r.bases += seq;
 }
@@ -83,6 +93,7 @@ void keep(Reads &r, uint32_t lib, const std::string &name, const std::string &se
 std::string load(const char *path, uint32_t lib, uint32_t minLen, Reads &r) {
   FILE *f = fopen(path, "rb");
   if (!f) return std::string("cannot open: ") + strerror(errno);
+  const size_t first = r.len.size();
   std::string line, name, seq, qual;
   bool        have = false;
   long        lineNo = 0;
@@ -140,6 +151,10 @@ std::string load(const char *path, uint32_t lib, uint32_t minLen, Reads &r) {
   }
   if (err.empty() && have) keep(r, lib, name, seq, minLen);
   if (err.empty() && ferror(f)) err = std::string("read error: ") + strerror(errno);
+  for (size_t i = first; err.empty() && i < r.len.size(); i++)
+    if (r.len[i] > kMaxReadLen)
+      err = "read '" + r.names[i] + "' has " + std::to_string(r.len[i]) + " bases, more than the " +
+            std::to_string(kMaxReadLen) + " a read store holds";
   fclose(f);
   return err;
 }

@@ -97,3 +97,15 @@ def test_imported_reads_run_through_the_oracle(importer, oracle, golden_inputs, 
                        stderr=subprocess.DEVNULL)
         recs.append(oic.sort_records(np.fromfile(o, dtype=np.uint32).reshape(-1, 6)))
     assert len(recs[0]) > 1000 and recs[0].shape == recs[1].shape and (recs[0] == recs[1]).all()
+
+
+def test_read_longer_than_a_store_holds_is_rejected(importer, tmp_path):
+    fa = tmp_path / "long.fa"
+    fa.write_text(">ok\nACGT\n>huge\n" + "A" * ((1 << 21) - 1) + "C\n")
+    out = str(tmp_path / "r.seqdb")
+    r = run(importer, "-o", out, str(fa))
+    assert r.returncode == 1 and "read 'huge' has 2097152 bases, more than the 2097151" in r.stderr
+    assert not os.path.exists(out)
+    fa.write_text(">ok\nACGT\n>edge\n" + "A" * ((1 << 21) - 1) + "\n")
+    assert run(importer, "-o", out, str(fa)).returncode == 0
+    assert [len(s) for _, s in reads_of(out)] == [4, (1 << 21) - 1]
